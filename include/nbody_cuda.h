@@ -1,0 +1,199 @@
+/*
+ * nbody_cuda -- C ABI of the GB300 (sm_103a) N-body solver.
+ *
+ * This is the device layer a CUDA solver variant of stett/nbody binds. It stands where
+ * the Vulkan device layer stands for the reference's GPU variants (source/gpu.h:72-353):
+ * the reference's Solver implementations (source/solvers/gpu_solver*.h) call
+ * GpuDevice::{reserve_bodies, map_bodies, step, accelerate, integrate, download}; the
+ * CUDA solver (nbody_gb300/host/cuda_solver.h) calls the functions below instead.
+ *
+ * Conventions
+ *   - Plain C: no exceptions cross this boundary; every call returns an nbody_status and
+ *     nbody_cuda_last_error() describes the most recent failure on a context.
+ *   - Host memory is caller-owned. Device memory belongs to the context, except for the
+ *     nbody_cuda_dev_* entry points, which work on caller-owned device buffers.
+ *   - Body records are the reference's 48-byte Body (include/nbody/body.h:6-19):
+ *       float pos[3], radius, vel[3], mass, acc[3], pad.
+ *     The split layout is the reference's three 16-byte streams (source/gpu.h:32-48):
+ *       pos_mass {x, y, z, m}, vel_radius {vx, vy, vz, r}, acc {ax, ay, az, 0}.
+ *   - One context is used from one host thread at a time (the reference's Sim is
+ *     single-threaded, source/sim.cpp:86-90). Work is queued on the context's stream and
+ *     only synchronised where a result must reach the host.
+ */
+#ifndef NBODY_CUDA_H
+#define NBODY_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBODY_CUDA_ABI_VERSION 1
+
+typedef enum nbody_status
+{
+    NBODY_OK = 0,
+    NBODY_ERR_INVALID = 1,      /* a bad argument; nothing was queued */
+    NBODY_ERR_NO_DEVICE = 2,    /* no usable CUDA device */
+    NBODY_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+    NBODY_ERR_ALLOC = 4,        /* device or pinned host allocation failed */
+    NBODY_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+    NBODY_ERR_UNSUPPORTED = 6   /* a parameter combination this build does not provide */
+} nbody_status;
+
+/* Force summation mode; mirrors nbody::Mode (source/gpu.h:13). */
+typedef enum nbody_mode
+{
+    NBODY_MODE_N2 = 0,          /* direct summation (the reference's brute force) */
+    NBODY_MODE_NLOGN = 1        /* Barnes-Hut tree */
+} nbody_mode;
+
+/* Force law. CUTOFF is the reference's (source/detail/physics.h:21-42): a pair
+ * contributes nothing when |d|^2 <= radius_target^2, else G*m*d/|d|^3.
+ * SOFTENED is G*m*d/(|d|^2 + eps2)^(3/2) and needs eps2 > 0. */
+typedef enum nbody_law
+{
+    NBODY_LAW_CUTOFF = 0,
+    NBODY_LAW_SOFTENED = 1
+} nbody_law;
+
+/* Arithmetic of the force sum and the integrator.
+ * FP32: FP32 throughout (the reference's arithmetic).
+ * COMPENSATED: FP32 pair forces; per-tile FP32 partials Kahan-summed, chunk partials
+ *   summed in FP64; positions kept as an FP64 origin plus FP32 offsets with Kahan
+ *   compensation of the position and velocity updates.
+ * FP64: FP64 throughout (direct summation only). */
+typedef enum nbody_precision
+{
+    NBODY_PREC_FP32 = 0,
+    NBODY_PREC_COMPENSATED = 1,
+    NBODY_PREC_FP64 = 2
+} nbody_precision;
+
+/* Device-side body layout of a context: the reference's two GPU layouts. */
+typedef enum nbody_layout
+{
+    NBODY_LAYOUT_SOA = 0,       /* split streams, as GpuSolverSplit (gpu_solver_split.h) */
+    NBODY_LAYOUT_AOS = 1        /* interleaved Body, as GpuSolver (gpu_solver.h) */
+} nbody_layout;
+
+/* Which streams a download brings back; mirrors nbody::Readback (source/gpu.h:52-58). */
+enum
+{
+    NBODY_READ_POSITIONS = 1u << 0,     /* pos and mass */
+    NBODY_READ_VELOCITIES = 1u << 1,    /* vel and radius */
+    NBODY_READ_ACCELERATIONS = 1u << 2,
+    NBODY_READ_ALL = 7u
+};
+
+/* Per-step parameters; the fields of nbody::PushConstants (source/gpu.h:17-27) that a
+ * step reads, plus the law/precision selection the reference does not have. */
+typedef struct nbody_step_params
+{
+    float dt;           /* time step */
+    float theta;        /* Barnes-Hut opening parameter, reference convention:
+                           a cell is accepted when |com - x|^2 > size^2 * theta^2 */
+    float G;            /* gravitational constant (State::gravity) */
+    float eps2;         /* softening length squared (SOFTENED law only) */
+    float size;         /* world edge (State::size): wrap period and Barnes-Hut root box */
+    int32_t wrap;       /* nonzero: wrap positions into [-size/2, size/2] (State::wrap) */
+    int32_t mode;       /* nbody_mode */
+    int32_t law;        /* nbody_law */
+    int32_t precision;  /* nbody_precision */
+    int32_t reserved[3];/* zero */
+} nbody_step_params;
+
+typedef struct nbody_cuda nbody_cuda;
+
+/* --- device discovery and lifetime ------------------------------------------------- */
+
+/* Probe for a usable sm_103 device without creating a context. Returns NBODY_OK, or a
+ * status with the reason written to `why`. Replaces GpuDevice::probe (source/gpu.cpp:115-149). */
+int nbody_cuda_probe(char* why, size_t why_len);
+
+/* Create a context on the current CUDA device with the given body layout. Replaces
+ * constructing GpuDevice (source/gpu.cpp, via Context::require_gpu, source/sim.cpp:129-136). */
+int nbody_cuda_create(nbody_cuda** out, int layout);
+void nbody_cuda_destroy(nbody_cuda* ctx);
+
+/* Copy the description of the last failure on `ctx` (or of the last failed create when
+ * ctx is NULL) into buf. Returns the status of that failure. */
+int nbody_cuda_last_error(const nbody_cuda* ctx, char* buf, size_t len);
+
+/* Queue work on `stream` (a cudaStream_t) instead of the context's own stream. NULL
+ * restores the context's own stream. */
+int nbody_cuda_set_stream(nbody_cuda* ctx, void* stream);
+void* nbody_cuda_stream(const nbody_cuda* ctx);
+int nbody_cuda_layout(const nbody_cuda* ctx);
+
+/* --- bodies ---------------------------------------------------------------------------- */
+
+/* Grow device storage to hold at least n bodies. Replaces GpuDevice::reserve_bodies. */
+int nbody_cuda_reserve(nbody_cuda* ctx, size_t n);
+size_t nbody_cuda_count(const nbody_cuda* ctx);
+
+/* Replace the device bodies with n host Body records (48 B each). The device copy is
+ * split or kept interleaved per the context layout. Replaces the upload half of
+ * GpuSolverSplit::upload_bodies / GpuSolver::upload (gpu_solver_split.h:155-177). */
+int nbody_cuda_upload_bodies(nbody_cuda* ctx, const void* bodies, size_t n);
+
+/* Write the streams selected by `mask` into n host Body records; fields not selected
+ * are left untouched. Reads min(n, count) bodies (gpu_solver_split.h:202). Synchronous.
+ * Replaces GpuDevice::download + the re-interleave in materialize(). */
+int nbody_cuda_download_bodies(nbody_cuda* ctx, void* bodies, size_t n, unsigned mask);
+
+/* Split-stream transfers (16 B per body per stream); NULL pointers are skipped. */
+int nbody_cuda_upload_soa(nbody_cuda* ctx, const float* pos_mass, const float* vel_radius,
+                          const float* acc, size_t n);
+int nbody_cuda_download_soa(nbody_cuda* ctx, float* pos_mass, float* vel_radius, float* acc,
+                            size_t n);
+
+/* --- stepping (queued, asynchronous) --------------------------------------------------- */
+
+/* Accelerations for every body. Replaces GpuDevice::accelerate (source/gpu.cpp:799-841). */
+int nbody_cuda_accelerate(nbody_cuda* ctx, const nbody_step_params* p);
+/* Semi-implicit Euler v += a*dt; x += v*dt; optional wrap (physics.h:60-70).
+ * Replaces GpuDevice::integrate. */
+int nbody_cuda_integrate(nbody_cuda* ctx, const nbody_step_params* p);
+/* `steps` x (accelerate; integrate), fused where possible. Replaces GpuDevice::step
+ * (source/gpu.cpp:842-875) and Solver::update (source/solver.h:59). */
+int nbody_cuda_update(nbody_cuda* ctx, const nbody_step_params* p, int steps);
+/* Wait for queued work; reports a device-side error (e.g. NBODY_ERR_TIMEOUT). */
+int nbody_cuda_synchronize(nbody_cuda* ctx);
+
+/* --- caller-owned device buffers (no context storage, no allocation by the call
+ *     beyond the context's scratch) ------------------------------------------------------ */
+
+/* Direct-sum accelerations over split streams already resident on the device:
+ * pos_mass, vel_radius (radius read for the CUTOFF law only), acc out; n bodies.
+ * The device twin of accelerate_split.comp N2 mode (shaders/accelerate_split.comp:9-18). */
+int nbody_cuda_dev_accel_soa(nbody_cuda* ctx, const void* pos_mass, const void* vel_radius,
+                             void* acc, size_t n, const nbody_step_params* p);
+/* Same over interleaved 48-byte Body records (shaders/accelerate.comp:9-17); writes
+ * Body::acc. */
+int nbody_cuda_dev_accel_aos(nbody_cuda* ctx, void* bodies, size_t n,
+                             const nbody_step_params* p);
+/* Semi-implicit Euler over split streams (shaders/integrate_split.comp). */
+int nbody_cuda_dev_integrate_soa(nbody_cuda* ctx, void* pos_mass, void* vel_radius,
+                                 const void* acc, size_t n, const nbody_step_params* p);
+
+/* --- introspection ------------------------------------------------------------------- */
+
+/* Kernel launches this context queued since creation (all entry points). */
+uint64_t nbody_cuda_launch_count(const nbody_cuda* ctx);
+/* Last direct-sum launch shape: targets per thread, threads per block, source tile,
+ * j-split count and grid size (for the bench's roofline arithmetic and for tests). */
+int nbody_cuda_last_direct_config(const nbody_cuda* ctx, int* targets_per_thread,
+                                  int* block, int* tile, int* jsplit, int* grid);
+
+/* Measured FP32 multiply-add throughput of this device in TFLOP/s (2 flop per lane per
+ * FFMA), scalar FFMA and packed FFMA2 chains; the denominator of the direct-sum
+ * roofline. Synchronous; takes well under a second. */
+int nbody_cuda_calibrate_fp32(nbody_cuda* ctx, double* tflops_scalar, double* tflops_packed);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,109 @@
+// Shared device helpers for the sm_103a kernels: bounded mbarrier waits, TMA bulk
+// copies, the packed FP32x2 arithmetic and the SFU reciprocal square root.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "nbody_cuda.h"
+
+namespace nbg
+{
+    // Device error word bits (ctx->dev_error). Kernels OR these in and return; the host
+    // reads the word at the next synchronisation point and maps it to a status.
+    enum : unsigned
+    {
+        DEV_ERR_TIMEOUT = 1u,   // a bounded mbarrier / flag wait gave up
+        DEV_ERR_BOUNDS = 2u,    // an index failed a bounds check and the access was skipped
+    };
+
+    // Limit on any spin-wait, in nanoseconds of %globaltimer. A tile copy completes in
+    // microseconds; a wait this long only ends when something is broken, and then the
+    // kernel reports DEV_ERR_TIMEOUT instead of hanging the device.
+    constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
+    __device__ __forceinline__ uint64_t globaltimer()
+    {
+        uint64_t t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        return t;
+    }
+
+    __device__ __forceinline__ uint32_t smem_addr(const void* p)
+    {
+        return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+    }
+
+    __device__ __forceinline__ void mbar_init(uint64_t* bar, const unsigned count)
+    {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(bar)), "r"(count) : "memory");
+    }
+
+    // Make mbarrier initialisation visible to the async (TMA) proxy.
+    __device__ __forceinline__ void fence_mbar_init()
+    {
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+
+    __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, const unsigned bytes)
+    {
+        asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;"
+                     :: "r"(smem_addr(bar)), "r"(bytes) : "memory");
+    }
+
+    __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, const unsigned parity)
+    {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+        return ok != 0;
+    }
+
+    // Wait for phase `parity` of `bar` to complete, giving up after kWaitLimitNs.
+    // Returns false on timeout (and records it in *err).
+    __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, const unsigned parity,
+                                                      unsigned* err)
+    {
+        if (mbar_try_wait(bar, parity))
+            return true;
+        const uint64_t start = globaltimer();
+        for (;;)
+        {
+            if (mbar_try_wait(bar, parity))
+                return true;
+            if (globaltimer() - start > kWaitLimitNs)
+            {
+                atomicOr(err, DEV_ERR_TIMEOUT);
+                return false;
+            }
+        }
+    }
+
+    // One-dimensional TMA bulk copy global -> shared, completing on `bar` with a byte
+    // count. dst, src and bytes must all be multiples of 16.
+    __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, const unsigned bytes,
+                                                uint64_t* bar)
+    {
+        asm volatile(
+            "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+            :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+    }
+
+    // MUFU reciprocal square root (approximate, flush-to-zero): one SFU instruction.
+    __device__ __forceinline__ float rsqrt_sfu(const float x)
+    {
+        float y;
+        asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+        return y;
+    }
+
+    __device__ __forceinline__ float2 f2(const float a) { return make_float2(a, a); }
+    __device__ __forceinline__ float2 add2(const float2 a, const float2 b) { return __fadd2_rn(a, b); }
+    __device__ __forceinline__ float2 mul2(const float2 a, const float2 b) { return __fmul2_rn(a, b); }
+    __device__ __forceinline__ float2 fma2(const float2 a, const float2 b, const float2 c) { return __ffma2_rn(a, b, c); }
+
+    inline unsigned ceil_div(const size_t a, const size_t b) { return static_cast<unsigned>((a + b - 1) / b); }
+}

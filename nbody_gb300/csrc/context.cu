@@ -1,0 +1,714 @@
+// The nbody_cuda context and the C ABI (include/nbody_cuda.h).
+//
+// A context owns the device copy of one simulation's bodies in one layout, a stream,
+// pinned staging for host transfers, the scratch the kernels need, and a device error
+// word. It plays the part GpuDevice plays for the reference's Vulkan variants
+// (source/gpu.h:72-353): grow-only buffers with a live count (gpu.h:76-80), uploads of
+// whole body arrays, downloads of selected streams (Readback, gpu.h:52-58).
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "common.cuh"
+#include "context.cuh"
+#include "direct.cuh"
+
+using namespace nbg;
+
+namespace
+{
+    thread_local std::string g_create_error;
+    thread_local int g_create_status = NBODY_OK;
+
+    int fail(nbody_cuda* ctx, const int status, const char* fmt, ...)
+    {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        std::vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        if (ctx)
+        {
+            ctx->last_error = buf;
+            ctx->last_status = status;
+        }
+        else
+        {
+            g_create_error = buf;
+            g_create_status = status;
+        }
+        if (std::getenv("NBODY_CUDA_VERBOSE"))
+            std::fprintf(stderr, "nbody_cuda: %s\n", buf);
+        return status;
+    }
+
+    int cuda_fail(nbody_cuda* ctx, const cudaError_t e, const char* what)
+    {
+        const int st = (e == cudaErrorMemoryAllocation) ? NBODY_ERR_ALLOC : NBODY_ERR_CUDA;
+        return fail(ctx, st, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+    }
+
+#define NBG_CUDA(ctx, call, what)                       \
+    do                                                  \
+    {                                                   \
+        const cudaError_t e_ = (call);                  \
+        if (e_ != cudaSuccess)                          \
+            return cuda_fail((ctx), e_, (what));        \
+    } while (0)
+
+    bool fault_injected(const char* what)
+    {
+        const char* f = std::getenv("NBODY_CUDA_FAULT");
+        return f && std::strcmp(f, what) == 0;
+    }
+
+    bool is_pinned(const void* p)
+    {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return false;
+        }
+        return a.type == cudaMemoryTypeHost;
+    }
+
+    int check_params(nbody_cuda* ctx, const nbody_step_params* p)
+    {
+        if (!p)
+            return fail(ctx, NBODY_ERR_INVALID, "null step parameters");
+        if (p->law != NBODY_LAW_CUTOFF && p->law != NBODY_LAW_SOFTENED)
+            return fail(ctx, NBODY_ERR_INVALID, "unknown force law %d", p->law);
+        if (p->law == NBODY_LAW_SOFTENED && !(p->eps2 > 0.f))
+            return fail(ctx, NBODY_ERR_INVALID, "the softened law needs eps2 > 0 (got %g)", p->eps2);
+        if (p->mode != NBODY_MODE_N2 && p->mode != NBODY_MODE_NLOGN)
+            return fail(ctx, NBODY_ERR_INVALID, "unknown mode %d", p->mode);
+        if (p->precision < NBODY_PREC_FP32 || p->precision > NBODY_PREC_FP64)
+            return fail(ctx, NBODY_ERR_INVALID, "unknown precision %d", p->precision);
+        return NBODY_OK;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// internal helpers shared with the other translation units
+// ---------------------------------------------------------------------------------------
+namespace nbg
+{
+    int ctx_fail(nbody_cuda* ctx, const int status, const char* msg)
+    {
+        return fail(ctx, status, "%s", msg);
+    }
+
+    int ctx_cuda_fail(nbody_cuda* ctx, const cudaError_t e, const char* what)
+    {
+        return cuda_fail(ctx, e, what);
+    }
+
+    int ensure_scratch(nbody_cuda* ctx, const size_t bytes)
+    {
+        if (bytes <= ctx->scratch_bytes)
+            return NBODY_OK;
+        if (fault_injected("alloc"))
+            return fail(ctx, NBODY_ERR_ALLOC, "injected allocation failure (NBODY_CUDA_FAULT=alloc)");
+        if (ctx->scratch)
+            cudaFreeAsync(ctx->scratch, ctx->stream);
+        ctx->scratch = nullptr;
+        ctx->scratch_bytes = 0;
+        const size_t grow = std::max(bytes, ctx->scratch_bytes + ctx->scratch_bytes / 2);
+        NBG_CUDA(ctx, cudaMallocAsync(&ctx->scratch, grow, ctx->stream), "scratch allocation");
+        ctx->scratch_bytes = grow;
+        return NBODY_OK;
+    }
+
+    int check_device_error(nbody_cuda* ctx)
+    {
+        unsigned word = 0;
+        NBG_CUDA(ctx, cudaMemcpyAsync(&word, ctx->dev_error, sizeof word, cudaMemcpyDeviceToHost, ctx->stream),
+                 "device error word readback");
+        NBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "stream synchronize");
+        if (!word)
+            return NBODY_OK;
+        NBG_CUDA(ctx, cudaMemsetAsync(ctx->dev_error, 0, sizeof(unsigned), ctx->stream), "error word reset");
+        if (word & DEV_ERR_TIMEOUT)
+            return fail(ctx, NBODY_ERR_TIMEOUT, "a bounded device wait timed out (device error word 0x%x)", word);
+        return fail(ctx, NBODY_ERR_CUDA, "device-side check failed (device error word 0x%x)", word);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------------------
+extern "C" {
+
+int nbody_cuda_probe(char* why, const size_t why_len)
+{
+    auto say = [&](const char* msg) {
+        if (why && why_len)
+        {
+            std::strncpy(why, msg, why_len - 1);
+            why[why_len - 1] = 0;
+        }
+    };
+    if (fault_injected("nodevice"))
+    {
+        say("injected: no CUDA device (NBODY_CUDA_FAULT=nodevice)");
+        return NBODY_ERR_NO_DEVICE;
+    }
+    int count = 0;
+    const cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0)
+    {
+        char buf[256];
+        std::snprintf(buf, sizeof buf, "no CUDA device: %s", e != cudaSuccess ? cudaGetErrorString(e) : "none found");
+        cudaGetLastError();
+        say(buf);
+        return NBODY_ERR_NO_DEVICE;
+    }
+    int dev = 0, major = 0, minor = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    if (major != 10 || minor != 3)
+    {
+        char buf[256];
+        std::snprintf(buf, sizeof buf, "device %d is sm_%d%d; this build is for sm_103a (GB300) only", dev, major, minor);
+        say(buf);
+        return NBODY_ERR_UNSUPPORTED;
+    }
+    say("");
+    return NBODY_OK;
+}
+
+int nbody_cuda_create(nbody_cuda** out, const int layout)
+{
+    if (!out)
+        return fail(nullptr, NBODY_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    if (layout != NBODY_LAYOUT_SOA && layout != NBODY_LAYOUT_AOS)
+        return fail(nullptr, NBODY_ERR_INVALID, "unknown layout %d", layout);
+    char why[256];
+    const int st = nbody_cuda_probe(why, sizeof why);
+    if (st != NBODY_OK)
+        return fail(nullptr, st, "%s", why);
+    if (fault_injected("alloc"))
+        return fail(nullptr, NBODY_ERR_ALLOC, "injected allocation failure (NBODY_CUDA_FAULT=alloc)");
+
+    nbody_cuda* ctx = new (std::nothrow) nbody_cuda();
+    if (!ctx)
+        return fail(nullptr, NBODY_ERR_ALLOC, "host allocation failed");
+    ctx->layout = layout;
+    cudaGetDevice(&ctx->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&ctx->dev_error, sizeof(unsigned));
+    if (e == cudaSuccess)
+        e = cudaMemset(ctx->dev_error, 0, sizeof(unsigned));
+    if (e != cudaSuccess)
+    {
+        const int s = cuda_fail(nullptr, e, "context creation");
+        nbody_cuda_destroy(ctx);
+        return s;
+    }
+    ctx->stream = ctx->own_stream;
+    *out = ctx;
+    return NBODY_OK;
+}
+
+void nbody_cuda_destroy(nbody_cuda* ctx)
+{
+    if (!ctx)
+        return;
+    if (ctx->stream)
+        cudaStreamSynchronize(ctx->stream);
+    release_bh(ctx);
+    cudaFree(ctx->pm);
+    cudaFree(ctx->vr);
+    cudaFree(ctx->acc);
+    cudaFree(ctx->bodies);
+    cudaFree(ctx->aos_stage);
+    cudaFree(ctx->scratch);
+    cudaFree(ctx->dev_error);
+    cudaFreeHost(ctx->pinned);
+    if (ctx->pinned_event)
+        cudaEventDestroy(ctx->pinned_event);
+    if (ctx->own_stream)
+        cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+int nbody_cuda_last_error(const nbody_cuda* ctx, char* buf, const size_t len)
+{
+    const std::string& msg = ctx ? ctx->last_error : g_create_error;
+    if (buf && len)
+    {
+        std::strncpy(buf, msg.c_str(), len - 1);
+        buf[len - 1] = 0;
+    }
+    return ctx ? ctx->last_status : g_create_status;
+}
+
+int nbody_cuda_set_stream(nbody_cuda* ctx, void* stream)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    if (s != ctx->stream)
+    {
+        // Order the new stream after everything queued so far.
+        cudaEvent_t ev;
+        NBG_CUDA(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event create");
+        cudaEventRecord(ev, ctx->stream);
+        cudaStreamWaitEvent(s, ev, 0);
+        cudaEventDestroy(ev);
+        ctx->stream = s;
+    }
+    return NBODY_OK;
+}
+
+void* nbody_cuda_stream(const nbody_cuda* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
+int nbody_cuda_layout(const nbody_cuda* ctx) { return ctx ? ctx->layout : -1; }
+size_t nbody_cuda_count(const nbody_cuda* ctx) { return ctx ? ctx->count : 0; }
+uint64_t nbody_cuda_launch_count(const nbody_cuda* ctx) { return ctx ? ctx->launches : 0; }
+
+int nbody_cuda_last_direct_config(const nbody_cuda* ctx, int* T, int* block, int* tile, int* jsplit, int* grid)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    const DirectPlan& p = ctx->last_plan;
+    if (T) *T = p.T;
+    if (block) *block = p.block;
+    if (tile) *tile = p.tile;
+    if (jsplit) *jsplit = p.jsplit;
+    if (grid) *grid = p.grid_x * p.jsplit;
+    return NBODY_OK;
+}
+
+int nbody_cuda_reserve(nbody_cuda* ctx, const size_t n)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (n > static_cast<size_t>(INT32_MAX / 4))
+        return fail(ctx, NBODY_ERR_INVALID, "body count %zu exceeds this build's limit", n);
+    if (n <= ctx->cap)
+        return NBODY_OK;
+    if (fault_injected("alloc"))
+        return fail(ctx, NBODY_ERR_ALLOC, "injected allocation failure (NBODY_CUDA_FAULT=alloc)");
+    // Grow-only with headroom (Buffer::reserve, gpu.h:101-103); contents move with it.
+    const size_t cap = std::max(n, ctx->cap + ctx->cap / 2);
+    auto grow = [&](float4** p, const size_t per_body) -> int {
+        float4* q = nullptr;
+        NBG_CUDA(ctx, cudaMallocAsync(&q, cap * per_body, ctx->stream), "body storage allocation");
+        if (*p && ctx->count)
+            NBG_CUDA(ctx, cudaMemcpyAsync(q, *p, ctx->count * per_body, cudaMemcpyDeviceToDevice, ctx->stream), "body storage move");
+        if (*p)
+            cudaFreeAsync(*p, ctx->stream);
+        *p = q;
+        return NBODY_OK;
+    };
+    int st = NBODY_OK;
+    if (ctx->layout == NBODY_LAYOUT_SOA)
+    {
+        if ((st = grow(&ctx->pm, 16)) || (st = grow(&ctx->vr, 16)) || (st = grow(&ctx->acc, 16)))
+            return st;
+    }
+    else
+    {
+        float4* b = reinterpret_cast<float4*>(ctx->bodies);
+        if ((st = grow(&b, 48)))
+            return st;
+        ctx->bodies = reinterpret_cast<float*>(b);
+    }
+    ctx->cap = cap;
+    return NBODY_OK;
+}
+
+namespace
+{
+    // Pinned staging, reused across calls; waits for the previous transfer through it.
+    int staging(nbody_cuda* ctx, const size_t bytes, void** out)
+    {
+        if (ctx->pinned_event)
+            NBG_CUDA(ctx, cudaEventSynchronize(ctx->pinned_event), "staging wait");
+        else
+            NBG_CUDA(ctx, cudaEventCreateWithFlags(&ctx->pinned_event, cudaEventDisableTiming), "event create");
+        if (bytes > ctx->pinned_bytes)
+        {
+            cudaFreeHost(ctx->pinned);
+            ctx->pinned = nullptr;
+            ctx->pinned_bytes = 0;
+            NBG_CUDA(ctx, cudaMallocHost(&ctx->pinned, bytes), "pinned staging allocation");
+            ctx->pinned_bytes = bytes;
+        }
+        *out = ctx->pinned;
+        return NBODY_OK;
+    }
+
+    // Host -> device copy of `bytes` from `src`: straight from page-locked memory
+    // (waiting for it before returning, so the caller may reuse the buffer), or through
+    // the pinned staging buffer.
+    int h2d(nbody_cuda* ctx, void* dst, const void* src, const size_t bytes)
+    {
+        if (!bytes)
+            return NBODY_OK;
+        if (is_pinned(src))
+        {
+            NBG_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream), "host to device copy");
+            NBG_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "host to device copy");
+            return NBODY_OK;
+        }
+        void* stage = nullptr;
+        if (const int st = staging(ctx, bytes, &stage))
+            return st;
+        std::memcpy(stage, src, bytes);
+        NBG_CUDA(ctx, cudaMemcpyAsync(dst, stage, bytes, cudaMemcpyHostToDevice, ctx->stream), "host to device copy");
+        NBG_CUDA(ctx, cudaEventRecord(ctx->pinned_event, ctx->stream), "event record");
+        return NBODY_OK;
+    }
+
+    // Device -> host, synchronous.
+    int d2h(nbody_cuda* ctx, void* dst, const void* src, const size_t bytes)
+    {
+        if (!bytes)
+            return NBODY_OK;
+        if (is_pinned(dst))
+        {
+            NBG_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream), "device to host copy");
+            return check_device_error(ctx);
+        }
+        void* stage = nullptr;
+        if (const int st = staging(ctx, bytes, &stage))
+            return st;
+        NBG_CUDA(ctx, cudaMemcpyAsync(stage, src, bytes, cudaMemcpyDeviceToHost, ctx->stream), "device to host copy");
+        if (const int st = check_device_error(ctx))
+            return st;
+        std::memcpy(dst, stage, bytes);
+        return NBODY_OK;
+    }
+
+    int ensure_aos_stage(nbody_cuda* ctx, const size_t n)
+    {
+        if (n <= ctx->aos_stage_cap)
+            return NBODY_OK;
+        cudaFreeAsync(ctx->aos_stage, ctx->stream);
+        ctx->aos_stage = nullptr;
+        ctx->aos_stage_cap = 0;
+        NBG_CUDA(ctx, cudaMallocAsync(&ctx->aos_stage, n * 48, ctx->stream), "body staging allocation");
+        ctx->aos_stage_cap = n;
+        return NBODY_OK;
+    }
+}
+
+int nbody_cuda_upload_bodies(nbody_cuda* ctx, const void* bodies, const size_t n)
+{
+    if (!ctx || (!bodies && n))
+        return ctx ? fail(ctx, NBODY_ERR_INVALID, "null bodies") : NBODY_ERR_INVALID;
+    if (const int st = nbody_cuda_reserve(ctx, n))
+        return st;
+    ctx->count = n;
+    ctx->origin_valid = false;
+    if (!n)
+        return NBODY_OK;
+    if (ctx->layout == NBODY_LAYOUT_AOS)
+        return h2d(ctx, ctx->bodies, bodies, n * 48);
+    if (const int st = ensure_aos_stage(ctx, n))
+        return st;
+    if (const int st = h2d(ctx, ctx->aos_stage, bodies, n * 48))
+        return st;
+    NBG_CUDA(ctx, launch_split(ctx->aos_stage, ctx->pm, ctx->vr, ctx->acc, static_cast<int>(n), ctx->stream, &ctx->launches),
+             "split launch");
+    return NBODY_OK;
+}
+
+int nbody_cuda_download_bodies(nbody_cuda* ctx, void* bodies, const size_t n, const unsigned mask)
+{
+    if (!ctx || (!bodies && n))
+        return ctx ? fail(ctx, NBODY_ERR_INVALID, "null bodies") : NBODY_ERR_INVALID;
+    const size_t take = std::min(n, ctx->count);
+    if (!take || !(mask & NBODY_READ_ALL))
+        return check_device_error(ctx);
+    if (const int st = sync_precise_positions(ctx))
+        return st;
+    const float* dev = ctx->bodies;
+    if (ctx->layout == NBODY_LAYOUT_SOA)
+    {
+        if (const int st = ensure_aos_stage(ctx, take))
+            return st;
+        NBG_CUDA(ctx, launch_join(ctx->pm, ctx->vr, ctx->acc, ctx->aos_stage, static_cast<int>(take), ctx->stream, &ctx->launches),
+                 "join launch");
+        dev = ctx->aos_stage;
+    }
+    if ((mask & NBODY_READ_ALL) == NBODY_READ_ALL)
+        return d2h(ctx, bodies, dev, take * 48);
+    // Merge only the selected fields into the caller's records.
+    void* stage = nullptr;
+    if (const int st = staging(ctx, take * 48, &stage))
+        return st;
+    NBG_CUDA(ctx, cudaMemcpyAsync(stage, dev, take * 48, cudaMemcpyDeviceToHost, ctx->stream), "device to host copy");
+    if (const int st = check_device_error(ctx))
+        return st;
+    const float* s = static_cast<const float*>(stage);
+    float* d = static_cast<float*>(bodies);
+    for (size_t i = 0; i < take; ++i)
+    {
+        const float* si = s + 12 * i;
+        float* di = d + 12 * i;
+        if (mask & NBODY_READ_POSITIONS)
+        {
+            di[0] = si[0]; di[1] = si[1]; di[2] = si[2]; di[7] = si[7];
+        }
+        if (mask & NBODY_READ_VELOCITIES)
+        {
+            di[4] = si[4]; di[5] = si[5]; di[6] = si[6]; di[3] = si[3];
+        }
+        if (mask & NBODY_READ_ACCELERATIONS)
+        {
+            di[8] = si[8]; di[9] = si[9]; di[10] = si[10];
+        }
+    }
+    return NBODY_OK;
+}
+
+int nbody_cuda_upload_soa(nbody_cuda* ctx, const float* pos_mass, const float* vel_radius, const float* acc,
+                          const size_t n)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (ctx->layout != NBODY_LAYOUT_SOA)
+        return fail(ctx, NBODY_ERR_INVALID, "split-stream upload on an interleaved context");
+    if (const int st = nbody_cuda_reserve(ctx, n))
+        return st;
+    ctx->count = n;
+    ctx->origin_valid = false;
+    int st = NBODY_OK;
+    if (pos_mass && (st = h2d(ctx, ctx->pm, pos_mass, n * 16)))
+        return st;
+    if (vel_radius && (st = h2d(ctx, ctx->vr, vel_radius, n * 16)))
+        return st;
+    if (acc && (st = h2d(ctx, ctx->acc, acc, n * 16)))
+        return st;
+    return NBODY_OK;
+}
+
+int nbody_cuda_download_soa(nbody_cuda* ctx, float* pos_mass, float* vel_radius, float* acc, const size_t n)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (ctx->layout != NBODY_LAYOUT_SOA)
+        return fail(ctx, NBODY_ERR_INVALID, "split-stream download on an interleaved context");
+    const size_t take = std::min(n, ctx->count);
+    if (const int st = sync_precise_positions(ctx))
+        return st;
+    int st = NBODY_OK;
+    if (pos_mass && (st = d2h(ctx, pos_mass, ctx->pm, take * 16)))
+        return st;
+    if (vel_radius && (st = d2h(ctx, vel_radius, ctx->vr, take * 16)))
+        return st;
+    if (acc && (st = d2h(ctx, acc, ctx->acc, take * 16)))
+        return st;
+    return check_device_error(ctx);
+}
+
+int nbody_cuda_synchronize(nbody_cuda* ctx)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    return check_device_error(ctx);
+}
+
+// --- stepping --------------------------------------------------------------------------
+
+namespace
+{
+    int direct_accel(nbody_cuda* ctx, const nbody_step_params* p, const bool keep_partials)
+    {
+        const int n = static_cast<int>(ctx->count);
+        const bool aos = ctx->layout == NBODY_LAYOUT_AOS;
+        DirectPlan plan = plan_direct(ctx->count, p->law, aos, ctx->force_variant);
+        ctx->last_plan = plan;
+        if (plan.jsplit > 1)
+            if (const int st = ensure_scratch(ctx, static_cast<size_t>(plan.jsplit) * n * sizeof(float4)))
+                return st;
+        const float4* src = aos ? reinterpret_cast<const float4*>(ctx->bodies) : ctx->pm;
+        float4* scratch = static_cast<float4*>(ctx->scratch);
+        if (keep_partials && plan.jsplit > 1)
+        {
+            // The fused integrate sums the partials: launch the accelerate alone.
+            const cudaError_t e = launch_direct(plan, src, ctx->vr, ctx->acc, ctx->bodies, scratch, n, p->G,
+                                                p->eps2, ctx->dev_error, ctx->stream, &ctx->launches, false);
+            if (e != cudaSuccess)
+                return cuda_fail(ctx, e, "direct-sum launch");
+            ctx->pending_partials = plan.jsplit;
+            return NBODY_OK;
+        }
+        ctx->pending_partials = 0;
+        const cudaError_t e = launch_direct(plan, src, ctx->vr, ctx->acc, ctx->bodies, scratch, n, p->G, p->eps2,
+                                            ctx->dev_error, ctx->stream, &ctx->launches);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "direct-sum launch");
+        return NBODY_OK;
+    }
+
+    int do_integrate(nbody_cuda* ctx, const nbody_step_params* p)
+    {
+        const int n = static_cast<int>(ctx->count);
+        const float4* part = ctx->pending_partials > 1 ? static_cast<const float4*>(ctx->scratch) : nullptr;
+        const int js = ctx->pending_partials;
+        ctx->pending_partials = 0;
+        cudaError_t e;
+        if (ctx->layout == NBODY_LAYOUT_SOA)
+            e = launch_integrate_soa(ctx->pm, ctx->vr, ctx->acc, part, js, n, p->dt, p->size, p->wrap, ctx->stream,
+                                     &ctx->launches);
+        else
+            e = launch_integrate_aos(ctx->bodies, part, js, n, p->dt, p->size, p->wrap, ctx->stream, &ctx->launches);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "integrate launch");
+        return NBODY_OK;
+    }
+
+    int accelerate_impl(nbody_cuda* ctx, const nbody_step_params* p, const bool fuse_with_integrate)
+    {
+        if (p->precision == NBODY_PREC_COMPENSATED || p->precision == NBODY_PREC_FP64)
+            return precise_accelerate(ctx, p);
+        if (p->mode == NBODY_MODE_NLOGN)
+            return bh_accelerate(ctx, p);
+        return direct_accel(ctx, p, fuse_with_integrate);
+    }
+
+    int integrate_impl(nbody_cuda* ctx, const nbody_step_params* p)
+    {
+        if (p->precision == NBODY_PREC_COMPENSATED)
+            return precise_integrate(ctx, p);
+        if (const int st = sync_precise_positions(ctx))
+            return st;
+        return do_integrate(ctx, p);
+    }
+}
+
+int nbody_cuda_accelerate(nbody_cuda* ctx, const nbody_step_params* p)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    if (!ctx->count)
+        return NBODY_OK;
+    return accelerate_impl(ctx, p, false);
+}
+
+int nbody_cuda_integrate(nbody_cuda* ctx, const nbody_step_params* p)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    if (!ctx->count)
+        return NBODY_OK;
+    ctx->pending_partials = 0;
+    return integrate_impl(ctx, p);
+}
+
+int nbody_cuda_update(nbody_cuda* ctx, const nbody_step_params* p, const int steps)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    if (steps < 0)
+        return fail(ctx, NBODY_ERR_INVALID, "negative step count");
+    if (!ctx->count)
+        return NBODY_OK;
+    for (int s = 0; s < steps; ++s)
+    {
+        if (const int st = accelerate_impl(ctx, p, true))
+            return st;
+        if (const int st = integrate_impl(ctx, p))
+            return st;
+    }
+    return NBODY_OK;
+}
+
+// --- caller-owned device buffers -----------------------------------------------------------
+
+int nbody_cuda_dev_accel_soa(nbody_cuda* ctx, const void* pos_mass, const void* vel_radius, void* acc,
+                             const size_t n, const nbody_step_params* p)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    if (!n)
+        return NBODY_OK;
+    if (!pos_mass || !acc || (p->law == NBODY_LAW_CUTOFF && !vel_radius))
+        return fail(ctx, NBODY_ERR_INVALID, "null device buffer");
+    if ((reinterpret_cast<uintptr_t>(pos_mass) | reinterpret_cast<uintptr_t>(acc)) & 15u)
+        return fail(ctx, NBODY_ERR_INVALID, "device buffers must be 16-byte aligned");
+    if (n > static_cast<size_t>(INT32_MAX / 4))
+        return fail(ctx, NBODY_ERR_INVALID, "body count too large");
+    if (p->mode != NBODY_MODE_N2 || p->precision != NBODY_PREC_FP32)
+        return fail(ctx, NBODY_ERR_UNSUPPORTED, "caller-buffer accelerate is direct-sum FP32 only");
+    const DirectPlan plan = plan_direct(n, p->law, false, ctx->force_variant);
+    ctx->last_plan = plan;
+    if (plan.jsplit > 1)
+        if (const int st = ensure_scratch(ctx, static_cast<size_t>(plan.jsplit) * n * sizeof(float4)))
+            return st;
+    const cudaError_t e = launch_direct(plan, static_cast<const float4*>(pos_mass), static_cast<const float4*>(vel_radius),
+                                        static_cast<float4*>(acc), nullptr, static_cast<float4*>(ctx->scratch),
+                                        static_cast<int>(n), p->G, p->eps2, ctx->dev_error, ctx->stream, &ctx->launches);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "direct-sum launch");
+    return NBODY_OK;
+}
+
+int nbody_cuda_dev_accel_aos(nbody_cuda* ctx, void* bodies, const size_t n, const nbody_step_params* p)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    if (!n)
+        return NBODY_OK;
+    if (!bodies || (reinterpret_cast<uintptr_t>(bodies) & 15u))
+        return fail(ctx, NBODY_ERR_INVALID, "device body buffer must be non-null and 16-byte aligned");
+    if (n > static_cast<size_t>(INT32_MAX / 4))
+        return fail(ctx, NBODY_ERR_INVALID, "body count too large");
+    if (p->mode != NBODY_MODE_N2 || p->precision != NBODY_PREC_FP32)
+        return fail(ctx, NBODY_ERR_UNSUPPORTED, "caller-buffer accelerate is direct-sum FP32 only");
+    const DirectPlan plan = plan_direct(n, p->law, true, ctx->force_variant);
+    ctx->last_plan = plan;
+    if (plan.jsplit > 1)
+        if (const int st = ensure_scratch(ctx, static_cast<size_t>(plan.jsplit) * n * sizeof(float4)))
+            return st;
+    const cudaError_t e = launch_direct(plan, static_cast<const float4*>(bodies), nullptr, nullptr,
+                                        static_cast<float*>(bodies), static_cast<float4*>(ctx->scratch),
+                                        static_cast<int>(n), p->G, p->eps2, ctx->dev_error, ctx->stream, &ctx->launches);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "direct-sum launch");
+    return NBODY_OK;
+}
+
+int nbody_cuda_dev_integrate_soa(nbody_cuda* ctx, void* pos_mass, void* vel_radius, const void* acc,
+                                 const size_t n, const nbody_step_params* p)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    if (!n)
+        return NBODY_OK;
+    if (!pos_mass || !vel_radius || !acc)
+        return fail(ctx, NBODY_ERR_INVALID, "null device buffer");
+    if (n > static_cast<size_t>(INT32_MAX / 4))
+        return fail(ctx, NBODY_ERR_INVALID, "body count too large");
+    const cudaError_t e = launch_integrate_soa(static_cast<float4*>(pos_mass), static_cast<float4*>(vel_radius),
+                                               const_cast<float4*>(static_cast<const float4*>(acc)), nullptr, 0,
+                                               static_cast<int>(n), p->dt, p->size, p->wrap, ctx->stream, &ctx->launches);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "integrate launch");
+    return NBODY_OK;
+}
+
+} // extern "C"

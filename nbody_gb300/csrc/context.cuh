@@ -1,0 +1,81 @@
+// The nbody_cuda context (opaque in the C ABI) and the internal calls the translation
+// units make on it.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <cuda_runtime.h>
+
+#include "nbody_cuda.h"
+#include "direct.cuh"
+
+namespace nbg
+{
+    struct BhState;         // bh.cu
+    struct PreciseState;    // direct_precise.cu
+}
+
+struct nbody_cuda
+{
+    int layout = NBODY_LAYOUT_SOA;
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+
+    // Bodies: live count and capacity (bodies), grow-only.
+    size_t count = 0;
+    size_t cap = 0;
+    float4* pm = nullptr;       // SoA: {x, y, z, m}
+    float4* vr = nullptr;       // SoA: {vx, vy, vz, radius}
+    float4* acc = nullptr;      // SoA: {ax, ay, az, 0}
+    float* bodies = nullptr;    // AoS: 12 floats per body
+
+    // Device staging for interleaved transfers into a split context.
+    float* aos_stage = nullptr;
+    size_t aos_stage_cap = 0;
+
+    // Kernel scratch (j-split partials, sort buffers, ...), grow-only.
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    int pending_partials = 0;   // >1: scratch holds this many accelerate partials
+
+    // Pinned host staging for pageable transfers.
+    void* pinned = nullptr;
+    size_t pinned_bytes = 0;
+    cudaEvent_t pinned_event = nullptr;
+
+    unsigned* dev_error = nullptr;  // device error word (nbg::DEV_ERR_*)
+
+    // Split-precision state (direct_precise.cu): FP64 origin + FP32 offsets live on the
+    // device while origin_valid; the float positions in pm/bodies are refreshed from
+    // them before anything reads positions.
+    bool origin_valid = false;
+    nbg::PreciseState* precise = nullptr;
+    nbg::BhState* bh = nullptr;
+
+    int force_variant = -1;     // pins the direct-sum (T, block) table entry when >= 0
+    nbg::DirectPlan last_plan{};
+    uint64_t launches = 0;
+
+    std::string last_error;
+    int last_status = NBODY_OK;
+};
+
+namespace nbg
+{
+    int ctx_fail(nbody_cuda* ctx, int status, const char* msg);
+    int ctx_cuda_fail(nbody_cuda* ctx, cudaError_t e, const char* what);
+    int ensure_scratch(nbody_cuda* ctx, size_t bytes);
+    int check_device_error(nbody_cuda* ctx);
+
+    // direct_precise.cu
+    int precise_accelerate(nbody_cuda* ctx, const nbody_step_params* p);
+    int precise_integrate(nbody_cuda* ctx, const nbody_step_params* p);
+    int sync_precise_positions(nbody_cuda* ctx);
+    void release_precise(nbody_cuda* ctx);
+
+    // bh.cu
+    int bh_accelerate(nbody_cuda* ctx, const nbody_step_params* p);
+    void release_bh(nbody_cuda* ctx);
+}

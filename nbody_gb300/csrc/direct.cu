@@ -1,0 +1,391 @@
+// Direct-sum accelerations (the reference's N^2 mode) for sm_103a.
+//
+// Reference behaviour restated: a_i = sum_j G*m_j*d_ij/|d_ij|^3 with the radius cutoff of
+// source/detail/physics.h:21-42 (CUTOFF law), or softened by eps2 (SOFTENED law). The
+// reference's GPU form is one invocation per target over plain SSBO loads
+// (shaders/accelerate.comp:9-17, accelerate_split.comp:9-18); its CPU form skips j == i
+// (source/solvers/cpu_brute_force.h:32-35). Here self-pairs contribute exactly zero under
+// both laws (d = 0 is cut off, or multiplied out by d), so no index test is needed.
+//
+// Kernel shape (GB300):
+//   - a CTA owns BLOCK*T targets: thread t holds targets base + t + k*BLOCK, k < T, in
+//     registers as T/2 packed FP32x2 pairs, so every pair interaction issues as
+//     3 FADD2 + 3 FFMA2 + 2 MUFU.RSQ + 3 FMUL2 + 3 FFMA2 for two targets.
+//   - sources stream through shared memory in TILE-body tiles, STAGES deep, each tile
+//     one TMA bulk copy (cp.async.bulk) completing on an mbarrier; every thread reads
+//     the same source (a broadcast shared load) and applies it to its T targets.
+//   - the source range can be split into `jsplit` chunks (blockIdx.y) so that the grid
+//     fills the 152 SMs evenly; chunk partials go to a scratch array and are summed in
+//     a fixed order (deterministic) by reduce_partials or the fused integrate.
+#include <algorithm>
+#include <cstdio>
+
+#include "common.cuh"
+#include "direct.cuh"
+
+namespace nbg
+{
+    // One source (sx, sy, sz, sm) applied to two targets held as negated positions.
+    template <int LAW>
+    __device__ __forceinline__ void interact2(const float2 sx, const float2 sy, const float2 sz,
+                                              const float2 sm, const float2 nx, const float2 ny,
+                                              const float2 nz, const float2 lim, float2& ax,
+                                              float2& ay, float2& az)
+    {
+        const float2 dx = add2(sx, nx);
+        const float2 dy = add2(sy, ny);
+        const float2 dz = add2(sz, nz);
+        float2 r2 = (LAW == NBODY_LAW_SOFTENED) ? fma2(dx, dx, lim) : mul2(dx, dx);
+        r2 = fma2(dy, dy, r2);
+        r2 = fma2(dz, dz, r2);
+        float2 inv = make_float2(rsqrt_sfu(r2.x), rsqrt_sfu(r2.y));
+        if (LAW == NBODY_LAW_CUTOFF)
+        {
+            // physics.h:38-39: nothing when |d|^2 <= radius^2 (lim holds radius^2)
+            inv.x = r2.x > lim.x ? inv.x : 0.f;
+            inv.y = r2.y > lim.y ? inv.y : 0.f;
+        }
+        const float2 inv2 = mul2(inv, inv);
+        const float2 mi = mul2(sm, inv);
+        const float2 s = mul2(mi, inv2);
+        ax = fma2(dx, s, ax);
+        ay = fma2(dy, s, ay);
+        az = fma2(dz, s, az);
+    }
+
+    // Source records: SoA streams one float4 {x,y,z,m} per body; AoS streams the whole
+    // 48-byte Body (3 float4: {pos, radius}, {vel, mass}, {acc, pad}).
+    template <bool AOS>
+    struct Layout
+    {
+        static constexpr int kRec = AOS ? 3 : 1;
+    };
+
+    template <int T, int BLOCK, int TILE, int STAGES, int LAW, bool AOS>
+    __global__ void __launch_bounds__(BLOCK, (T >= 8 ? 2 : 3))
+    direct_fp32_kernel(const float4* __restrict__ src,        // pos_mass (SoA) or Body (AoS)
+                       const float4* __restrict__ vel_radius, // SoA radius source (CUTOFF)
+                       float4* __restrict__ out,              // acc (SoA) / partials
+                       float* __restrict__ body_out,          // AoS Body array to write acc
+                       const int n, const int chunk, const float G, const float eps2,
+                       unsigned* __restrict__ err)
+    {
+        constexpr int P = T / 2;
+        constexpr int REC = Layout<AOS>::kRec;
+        __shared__ __align__(128) float4 tile[STAGES][TILE * REC];
+        __shared__ __align__(8) uint64_t bar[STAGES];
+
+        const int tid = threadIdx.x;
+        const int base = blockIdx.x * (BLOCK * T);
+        const int j0 = blockIdx.y * chunk;
+        const int j1 = min(n, j0 + chunk);
+        const int ntiles = (j1 > j0) ? (j1 - j0 + TILE - 1) / TILE : 0;
+
+        if (tid == 0)
+        {
+            for (int s = 0; s < STAGES; ++s)
+                mbar_init(&bar[s], 1);
+            fence_mbar_init();
+        }
+        __syncthreads();
+
+        auto issue = [&](const int stage, const int t) {
+            const int first = j0 + t * TILE;
+            const int cnt = min(TILE, j1 - first);
+            const unsigned bytes = static_cast<unsigned>(cnt) * 16u * REC;
+            mbar_arrive_expect_tx(&bar[stage], bytes);
+            tma_load_1d(&tile[stage][0], src + static_cast<size_t>(first) * REC, bytes, &bar[stage]);
+        };
+        if (tid == 0)
+            for (int s = 0; s < STAGES && s < ntiles; ++s)
+                issue(s, s);
+
+        // Targets: negated positions (so d = s + (-x)) and the cutoff radius^2 or eps^2.
+        float2 nx[P], ny[P], nz[P], lim[P], ax[P], ay[P], az[P];
+#pragma unroll
+        for (int p = 0; p < P; ++p)
+        {
+            float q[2][4];
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+            {
+                const int i = min(base + tid + (2 * p + h) * BLOCK, n - 1);
+                const float4 x = src[static_cast<size_t>(i) * REC];
+                q[h][0] = -x.x;
+                q[h][1] = -x.y;
+                q[h][2] = -x.z;
+                if (LAW == NBODY_LAW_CUTOFF)
+                {
+                    const float r = AOS ? x.w : vel_radius[i].w;
+                    q[h][3] = r * r;
+                }
+                else
+                    q[h][3] = eps2;
+            }
+            nx[p] = make_float2(q[0][0], q[1][0]);
+            ny[p] = make_float2(q[0][1], q[1][1]);
+            nz[p] = make_float2(q[0][2], q[1][2]);
+            lim[p] = make_float2(q[0][3], q[1][3]);
+            ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
+        }
+
+        int failed_at = -1;
+        for (int t = 0; t < ntiles; ++t)
+        {
+            const int stage = t % STAGES;
+            const bool ok = mbar_wait_bounded(&bar[stage], (t / STAGES) & 1u, err);
+            if (__syncthreads_or(!ok))
+            {
+                failed_at = t;
+                break;
+            }
+            const int cnt = min(TILE, j1 - (j0 + t * TILE));
+            if (cnt < TILE)
+            {
+                // Last, partial tile: pad with massless sources at the origin, which
+                // contribute exactly zero under both laws. The copy only wrote [0, cnt).
+                for (int k = cnt * REC + tid; k < TILE * REC; k += BLOCK)
+                    tile[stage][k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                __syncthreads();
+            }
+            const float4* tl = tile[stage];
+#pragma unroll 2
+            for (int j = 0; j < TILE; ++j)
+            {
+                const float4 s = tl[j * REC];
+                const float m = AOS ? tl[j * REC + 1].w : s.w;
+                const float2 sx = f2(s.x), sy = f2(s.y), sz = f2(s.z), sm = f2(m);
+#pragma unroll
+                for (int p = 0; p < P; ++p)
+                    interact2<LAW>(sx, sy, sz, sm, nx[p], ny[p], nz[p], lim[p], ax[p], ay[p], az[p]);
+            }
+            __syncthreads();
+            if (tid == 0 && t + STAGES < ntiles)
+                issue(stage, t + STAGES);
+        }
+        if (failed_at >= 0)
+        {
+            // Let the copies still in flight (tiles failed_at .. failed_at+STAGES-1) land,
+            // each with a bounded wait, before the CTA's shared memory goes away.
+            if (tid == 0)
+                for (int t = failed_at; t < ntiles && t < failed_at + STAGES; ++t)
+                    mbar_wait_bounded(&bar[t % STAGES], (t / STAGES) & 1u, err);
+            return;
+        }
+
+        const bool partial = gridDim.y > 1;
+#pragma unroll
+        for (int p = 0; p < P; ++p)
+        {
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+            {
+                const int i = base + tid + (2 * p + h) * BLOCK;
+                if (i >= n)
+                    continue;
+                const float a0 = G * (h ? ax[p].y : ax[p].x);
+                const float a1 = G * (h ? ay[p].y : ay[p].x);
+                const float a2 = G * (h ? az[p].y : az[p].x);
+                if (partial)
+                    out[static_cast<size_t>(blockIdx.y) * n + i] = make_float4(a0, a1, a2, 0.f);
+                else if (AOS)
+                {
+                    float* b = body_out + static_cast<size_t>(i) * 12 + 8;
+                    b[0] = a0;
+                    b[1] = a1;
+                    b[2] = a2;
+                }
+                else
+                    out[i] = make_float4(a0, a1, a2, 0.f);
+            }
+        }
+    }
+
+    // Sum jsplit chunk partials in chunk order into acc (SoA float4) or Body::acc (AoS).
+    __global__ void reduce_partials_kernel(const float4* __restrict__ part, const int jsplit,
+                                           const int n, float4* __restrict__ acc,
+                                           float* __restrict__ body_out)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n)
+            return;
+        float4 a = part[i];
+        for (int s = 1; s < jsplit; ++s)
+        {
+            const float4 b = part[static_cast<size_t>(s) * n + i];
+            a.x += b.x;
+            a.y += b.y;
+            a.z += b.z;
+        }
+        if (body_out)
+        {
+            float* b = body_out + static_cast<size_t>(i) * 12 + 8;
+            b[0] = a.x;
+            b[1] = a.y;
+            b[2] = a.z;
+        }
+        else
+            acc[i] = make_float4(a.x, a.y, a.z, 0.f);
+    }
+
+    // ------------------------------------------------------------------------------
+    // Launch planning
+    // ------------------------------------------------------------------------------
+    namespace
+    {
+        constexpr int kTile = 256;
+        constexpr int kStages = 3;
+
+        using KernelFn = void (*)(const float4*, const float4*, float4*, float*, int, int, float,
+                                  float, unsigned*);
+
+        struct Variant
+        {
+            int T, block;
+            KernelFn fn[2][2];  // [law][aos]
+        };
+
+        template <int T, int B>
+        Variant make_variant()
+        {
+            Variant v;
+            v.T = T;
+            v.block = B;
+            v.fn[0][0] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_CUTOFF, false>;
+            v.fn[0][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_CUTOFF, true>;
+            v.fn[1][0] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, false>;
+            v.fn[1][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, true>;
+            return v;
+        }
+
+        const Variant* variants(int* count)
+        {
+            static const Variant v[] = {
+                make_variant<8, 256>(),
+                make_variant<4, 256>(),
+                make_variant<4, 128>(),
+                make_variant<2, 64>(),
+            };
+            *count = static_cast<int>(sizeof(v) / sizeof(v[0]));
+            return v;
+        }
+
+        int sm_count()
+        {
+            static int sms = [] {
+                int dev = 0, s = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
+                return s > 0 ? s : 1;
+            }();
+            return sms;
+        }
+
+        int occupancy(KernelFn fn, const int block)
+        {
+            int blocks = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block, 0) != cudaSuccess)
+                return 1;
+            return blocks > 0 ? blocks : 1;
+        }
+    }
+
+    DirectPlan plan_direct(const size_t n, const int law, const bool aos, const int force_variant)
+    {
+        DirectPlan plan{};
+        int nv = 0;
+        const Variant* vs = variants(&nv);
+        const int li = law == NBODY_LAW_SOFTENED ? 1 : 0;
+        const int ai = aos ? 1 : 0;
+        const int sms = sm_count();
+
+        int chosen = -1;
+        if (force_variant >= 0 && force_variant < nv)
+            chosen = force_variant;
+        else
+        {
+            // Largest register block whose (target blocks x max chunks) fills the GPU.
+            for (int k = 0; k < nv; ++k)
+            {
+                const size_t per = static_cast<size_t>(vs[k].T) * vs[k].block;
+                const size_t tb = (n + per - 1) / per;
+                const size_t max_js = std::max<size_t>(1, n / (kTile * 4));
+                const size_t slots = static_cast<size_t>(occupancy(vs[k].fn[li][ai], vs[k].block)) * sms;
+                if (tb * max_js >= slots)
+                {
+                    chosen = k;
+                    break;
+                }
+            }
+            if (chosen < 0)
+                chosen = nv - 1;
+        }
+        const Variant& v = vs[chosen];
+        const size_t per = static_cast<size_t>(v.T) * v.block;
+        const size_t tb = std::max<size_t>(1, (n + per - 1) / per);
+        const size_t slots = static_cast<size_t>(occupancy(v.fn[li][ai], v.block)) * sms;
+        // Split the sources so tb*js CTAs pack into whole waves: minimise the padded
+        // work ceil(tb*js/slots)*slots/(tb*js) per unit, preferring fewer chunks.
+        const size_t max_js = std::max<size_t>(1, std::min<size_t>(64, n / (kTile * 4)));
+        size_t best_js = 1;
+        double best_cost = 1e300;
+        for (size_t js = 1; js <= max_js; ++js)
+        {
+            const size_t ctas = tb * js;
+            const size_t waves = (ctas + slots - 1) / slots;
+            // time ~ waves * (work per CTA) = waves / js (work per CTA shrinks with js)
+            const double cost = static_cast<double>(waves) / static_cast<double>(js)
+                                * (1.0 + 0.002 * static_cast<double>(js));
+            if (cost < best_cost - 1e-12)
+            {
+                best_cost = cost;
+                best_js = js;
+            }
+        }
+        // Chunks hold whole tiles, so the last chunk is the only ragged one.
+        size_t chunk = (n + best_js - 1) / best_js;
+        chunk = (chunk + kTile - 1) / kTile * kTile;
+        const size_t js = std::max<size_t>(1, (n + chunk - 1) / chunk);
+
+        plan.variant = chosen;
+        plan.T = v.T;
+        plan.block = v.block;
+        plan.tile = kTile;
+        plan.jsplit = static_cast<int>(js);
+        plan.chunk = static_cast<int>(chunk);
+        plan.grid_x = static_cast<int>(tb);
+        plan.law = law;
+        plan.aos = aos;
+        return plan;
+    }
+
+    cudaError_t launch_direct(const DirectPlan& plan, const float4* src, const float4* vel_radius,
+                              float4* acc, float* body_out, float4* scratch, const int n,
+                              const float G, const float eps2, unsigned* err, cudaStream_t stream,
+                              uint64_t* launches, const bool reduce)
+    {
+        if (n <= 0)
+            return cudaSuccess;
+        int nv = 0;
+        const Variant* vs = variants(&nv);
+        const Variant& v = vs[plan.variant];
+        const KernelFn fn = v.fn[plan.law == NBODY_LAW_SOFTENED ? 1 : 0][plan.aos ? 1 : 0];
+        const dim3 grid(plan.grid_x, plan.jsplit);
+        float4* out = plan.jsplit > 1 ? scratch : acc;
+        fn<<<grid, v.block, 0, stream>>>(src, vel_radius, out, plan.aos ? body_out : nullptr, n,
+                                         plan.chunk, G, eps2, err);
+        ++*launches;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess || plan.jsplit <= 1 || !reduce)
+            return e;
+        return launch_reduce(scratch, plan.jsplit, n, acc, plan.aos ? body_out : nullptr, stream, launches);
+    }
+
+    cudaError_t launch_reduce(const float4* scratch, const int jsplit, const int n, float4* acc,
+                              float* body_out, cudaStream_t stream, uint64_t* launches)
+    {
+        reduce_partials_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(scratch, jsplit, n, acc, body_out);
+        ++*launches;
+        return cudaGetLastError();
+    }
+}

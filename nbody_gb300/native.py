@@ -1,0 +1,216 @@
+"""ctypes binding of the C ABI in ``include/nbody_cuda.h``.
+
+This is how Python (tests, bench) reaches the CUDA library; it adds no behaviour of its
+own. The library is loaded from ``nbody_gb300/lib/libnbody_cuda.so`` (built in-tree by
+``nbody_gb300/build.py``); if it is missing, :func:`lib` raises -- there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libnbody_cuda.so"
+
+# status codes (nbody_status)
+OK, ERR_INVALID, ERR_NO_DEVICE, ERR_CUDA, ERR_ALLOC, ERR_TIMEOUT, ERR_UNSUPPORTED = range(7)
+MODE_N2, MODE_NLOGN = 0, 1
+LAW_CUTOFF, LAW_SOFTENED = 0, 1
+PREC_FP32, PREC_COMPENSATED, PREC_FP64 = 0, 1, 2
+LAYOUT_SOA, LAYOUT_AOS = 0, 1
+READ_POSITIONS, READ_VELOCITIES, READ_ACCELERATIONS, READ_ALL = 1, 2, 4, 7
+
+# Every symbol include/nbody_cuda.h declares (checked by tests/test_boundary.py).
+EXPORTS = (
+    "nbody_cuda_probe", "nbody_cuda_create", "nbody_cuda_destroy", "nbody_cuda_last_error",
+    "nbody_cuda_set_stream", "nbody_cuda_stream", "nbody_cuda_layout", "nbody_cuda_reserve",
+    "nbody_cuda_count", "nbody_cuda_upload_bodies", "nbody_cuda_download_bodies",
+    "nbody_cuda_upload_soa", "nbody_cuda_download_soa", "nbody_cuda_accelerate",
+    "nbody_cuda_integrate", "nbody_cuda_update", "nbody_cuda_synchronize",
+    "nbody_cuda_dev_accel_soa", "nbody_cuda_dev_accel_aos", "nbody_cuda_dev_integrate_soa",
+    "nbody_cuda_launch_count", "nbody_cuda_last_direct_config", "nbody_cuda_calibrate_fp32",
+)
+
+
+class StepParams(C.Structure):
+    """nbody_step_params."""
+    _fields_ = [("dt", C.c_float), ("theta", C.c_float), ("G", C.c_float), ("eps2", C.c_float),
+                ("size", C.c_float), ("wrap", C.c_int32), ("mode", C.c_int32), ("law", C.c_int32),
+                ("precision", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+def params(dt=0.0, theta=0.5, G=1.0, eps2=0.0, size=10000.0, wrap=False, mode=MODE_N2,
+           law=LAW_CUTOFF, precision=PREC_FP32) -> StepParams:
+    return StepParams(dt, theta, G, eps2, size, int(bool(wrap)), mode, law, precision)
+
+
+class NbodyError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"nbody_cuda status {status}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded library; raises if it was not built (no fallback path exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with nbody_gb300.build.build()")
+    L = C.CDLL(str(LIB_PATH))
+    vp, sz, u = C.c_void_p, C.c_size_t, C.c_uint
+    P = C.POINTER(StepParams)
+    sig = {
+        "nbody_cuda_probe": ([C.c_char_p, sz], C.c_int),
+        "nbody_cuda_create": ([C.POINTER(vp), C.c_int], C.c_int),
+        "nbody_cuda_destroy": ([vp], None),
+        "nbody_cuda_last_error": ([vp, C.c_char_p, sz], C.c_int),
+        "nbody_cuda_set_stream": ([vp, vp], C.c_int),
+        "nbody_cuda_stream": ([vp], vp),
+        "nbody_cuda_layout": ([vp], C.c_int),
+        "nbody_cuda_reserve": ([vp, sz], C.c_int),
+        "nbody_cuda_count": ([vp], sz),
+        "nbody_cuda_upload_bodies": ([vp, vp, sz], C.c_int),
+        "nbody_cuda_download_bodies": ([vp, vp, sz, u], C.c_int),
+        "nbody_cuda_upload_soa": ([vp, vp, vp, vp, sz], C.c_int),
+        "nbody_cuda_download_soa": ([vp, vp, vp, vp, sz], C.c_int),
+        "nbody_cuda_accelerate": ([vp, P], C.c_int),
+        "nbody_cuda_integrate": ([vp, P], C.c_int),
+        "nbody_cuda_update": ([vp, P, C.c_int], C.c_int),
+        "nbody_cuda_synchronize": ([vp], C.c_int),
+        "nbody_cuda_dev_accel_soa": ([vp, vp, vp, vp, sz, P], C.c_int),
+        "nbody_cuda_dev_accel_aos": ([vp, vp, sz, P], C.c_int),
+        "nbody_cuda_dev_integrate_soa": ([vp, vp, vp, vp, sz, P], C.c_int),
+        "nbody_cuda_launch_count": ([vp], C.c_uint64),
+        "nbody_cuda_last_direct_config": ([vp] + [C.POINTER(C.c_int)] * 5, C.c_int),
+        "nbody_cuda_calibrate_fp32": ([vp, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def probe() -> tuple[int, str]:
+    buf = C.create_string_buffer(512)
+    st = lib().nbody_cuda_probe(buf, len(buf))
+    return st, buf.value.decode()
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """One nbody_cuda context (device bodies in one layout + stream + scratch)."""
+
+    def __init__(self, layout: int = LAYOUT_SOA):
+        h = C.c_void_p()
+        st = lib().nbody_cuda_create(C.byref(h), layout)
+        if st != OK:
+            buf = C.create_string_buffer(512)
+            lib().nbody_cuda_last_error(None, buf, len(buf))
+            raise NbodyError(st, buf.value.decode())
+        self.h = h
+        self.layout = layout
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().nbody_cuda_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def error(self) -> str:
+        buf = C.create_string_buffer(512)
+        lib().nbody_cuda_last_error(self.h, buf, len(buf))
+        return buf.value.decode()
+
+    def check(self, st: int):
+        if st != OK:
+            raise NbodyError(st, self.error())
+
+    # --- bodies -----------------------------------------------------------------
+    def upload_bodies(self, bodies: np.ndarray):
+        b = np.ascontiguousarray(bodies, np.float32)
+        assert b.ndim == 2 and b.shape[1] == 12
+        self.check(lib().nbody_cuda_upload_bodies(self.h, _ptr(b), len(b)))
+
+    def download_bodies(self, n: int | None = None, mask: int = READ_ALL, into: np.ndarray | None = None):
+        n = self.count() if n is None else n
+        out = np.zeros((n, 12), np.float32) if into is None else into
+        self.check(lib().nbody_cuda_download_bodies(self.h, _ptr(out), n, mask))
+        return out
+
+    def upload_soa(self, pos_mass, vel_radius=None, acc=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (pos_mass, vel_radius, acc)]
+        n = len(arrs[0])
+        self.check(lib().nbody_cuda_upload_soa(self.h, *map(_ptr, arrs), n))
+
+    def download_soa(self, n: int | None = None):
+        n = self.count() if n is None else n
+        out = [np.zeros((n, 4), np.float32) for _ in range(3)]
+        self.check(lib().nbody_cuda_download_soa(self.h, *map(_ptr, out), n))
+        return out
+
+    def count(self) -> int:
+        return int(lib().nbody_cuda_count(self.h))
+
+    def reserve(self, n: int):
+        self.check(lib().nbody_cuda_reserve(self.h, n))
+
+    # --- stepping -------------------------------------------------------------------
+    def accelerate(self, p: StepParams):
+        self.check(lib().nbody_cuda_accelerate(self.h, C.byref(p)))
+
+    def integrate(self, p: StepParams):
+        self.check(lib().nbody_cuda_integrate(self.h, C.byref(p)))
+
+    def update(self, p: StepParams, steps: int = 1):
+        self.check(lib().nbody_cuda_update(self.h, C.byref(p), steps))
+
+    def synchronize(self):
+        self.check(lib().nbody_cuda_synchronize(self.h))
+
+    def set_stream(self, stream: int | None):
+        self.check(lib().nbody_cuda_set_stream(self.h, None if not stream else C.c_void_p(stream)))
+
+    # --- caller-owned device buffers (integer device pointers) -------------------------------
+    def dev_accel_soa(self, pos_mass: int, vel_radius: int | None, acc: int, n: int, p: StepParams):
+        self.check(lib().nbody_cuda_dev_accel_soa(self.h, C.c_void_p(pos_mass),
+                                                  C.c_void_p(vel_radius) if vel_radius else None,
+                                                  C.c_void_p(acc), n, C.byref(p)))
+
+    def dev_accel_aos(self, bodies: int, n: int, p: StepParams):
+        self.check(lib().nbody_cuda_dev_accel_aos(self.h, C.c_void_p(bodies), n, C.byref(p)))
+
+    def dev_integrate_soa(self, pos_mass: int, vel_radius: int, acc: int, n: int, p: StepParams):
+        self.check(lib().nbody_cuda_dev_integrate_soa(self.h, C.c_void_p(pos_mass), C.c_void_p(vel_radius),
+                                                      C.c_void_p(acc), n, C.byref(p)))
+
+    # --- introspection -------------------------------------------------------------------------
+    def launches(self) -> int:
+        return int(lib().nbody_cuda_launch_count(self.h))
+
+    def calibrate_fp32(self) -> tuple[float, float]:
+        s, p = C.c_double(), C.c_double()
+        self.check(lib().nbody_cuda_calibrate_fp32(self.h, C.byref(s), C.byref(p)))
+        return s.value, p.value
+
+    def last_direct_config(self) -> dict:
+        v = [C.c_int() for _ in range(5)]
+        self.check(lib().nbody_cuda_last_direct_config(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("targets_per_thread", "block", "tile", "jsplit", "grid"), (x.value for x in v)))

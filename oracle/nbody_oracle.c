@@ -1,0 +1,682 @@
+/*
+ * CPU oracle for the N-body hot path -- TEST INFRASTRUCTURE ONLY (see nbody_oracle.h).
+ *
+ * Built with -O2 -ffp-contract=off -frounding-math so every float operation is the one
+ * written here, in the order written, on both x86-64 and aarch64: the FP32 restatement
+ * of the reference then reproduces the reference (compiled with the same flags) bit for
+ * bit, which tests/test_oracle.py checks against fixtures made from the reference.
+ */
+#include "nbody_oracle.h"
+
+#include <fenv.h>
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+#pragma STDC FENV_ACCESS ON
+
+/* ------------------------------------------------------------------------------------
+ * Fork-join helper: run fn(ctx, begin, end) over a block partition of [0, n).
+ * Plays the part of detail::parallel_blocks (source/detail/parallel.h:16-22).
+ * ---------------------------------------------------------------------------------- */
+typedef void (*orc_block_fn)(void* ctx, size_t begin, size_t end);
+
+typedef struct
+{
+    orc_block_fn fn;
+    void* ctx;
+    size_t begin, end;
+} orc_job;
+
+static void* orc_job_run(void* p)
+{
+    orc_job* j = (orc_job*)p;
+    j->fn(j->ctx, j->begin, j->end);
+    return NULL;
+}
+
+int orc_default_threads(void)
+{
+    long c = sysconf(_SC_NPROCESSORS_ONLN);
+    return c > 0 ? (int)c : 1;
+}
+
+static void orc_parallel(size_t n, int nthreads, orc_block_fn fn, void* ctx)
+{
+    if (n == 0)
+        return;
+    if (nthreads <= 0)
+        nthreads = orc_default_threads();
+    if ((size_t)nthreads > n)
+        nthreads = (int)n;
+    if (nthreads == 1)
+    {
+        fn(ctx, 0, n);
+        return;
+    }
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    orc_job* jobs = (orc_job*)malloc(sizeof(orc_job) * (size_t)nthreads);
+    const size_t base = n / (size_t)nthreads, rem = n % (size_t)nthreads;
+    size_t at = 0;
+    for (int t = 0; t < nthreads; ++t)
+    {
+        const size_t len = base + ((size_t)t < rem ? 1 : 0);
+        jobs[t].fn = fn;
+        jobs[t].ctx = ctx;
+        jobs[t].begin = at;
+        jobs[t].end = at + len;
+        at += len;
+    }
+    for (int t = 1; t < nthreads; ++t)
+        pthread_create(&th[t], NULL, orc_job_run, &jobs[t]);
+    orc_job_run(&jobs[0]);
+    for (int t = 1; t < nthreads; ++t)
+        pthread_join(th[t], NULL);
+    free(jobs);
+    free(th);
+}
+
+/* ------------------------------------------------------------------------------------
+ * Force law: source/detail/physics.h:21-42.
+ * delta = src - pos; |delta|^2 = (dx*dx + dy*dy) + dz*dz (Vector dot, source/vector.cpp:10-13);
+ * zero when |delta|^2 <= radius^2; else ((G*m) * delta) / (sqrt(|delta|^2) * |delta|^2).
+ * ---------------------------------------------------------------------------------- */
+void orc_gravity(const float pos[3], const float radius, const float src[3],
+                 const float src_mass, const float G, float out[3])
+{
+    const float dx = src[0] - pos[0];
+    const float dy = src[1] - pos[1];
+    const float dz = src[2] - pos[2];
+    const float dsq = (dx * dx + dy * dy) + dz * dz;
+    const float rsq = radius * radius;
+    if (dsq <= rsq)
+    {
+        out[0] = out[1] = out[2] = 0.f;
+        return;
+    }
+    const float s = G * src_mass;
+    const float den = sqrtf(dsq) * dsq;
+    out[0] = (s * dx) / den;
+    out[1] = (s * dy) / den;
+    out[2] = (s * dz) / den;
+}
+
+/* Wrap into [-size/2, size/2]: physics.h:50-58 (double fmod, as the reference writes it). */
+float orc_wrap(const float x, const float size)
+{
+    if (size <= 0.f)
+        return x;
+    const float half = size * .5f;
+    return fmodf(fmodf(x + half, size) + size, size) - half;
+}
+
+/* Semi-implicit Euler: physics.h:60-70, run over all bodies as cpu_solver.h:29-42. */
+void orc_integrate(float* b, const size_t n, const float dt, const float size, const int wrap)
+{
+    for (size_t i = 0; i < n; ++i)
+    {
+        float* p = b + 12 * i;
+        for (int a = 0; a < 3; ++a)
+            p[4 + a] = p[4 + a] + p[8 + a] * dt;
+        for (int a = 0; a < 3; ++a)
+            p[a] = p[a] + p[4 + a] * dt;
+        if (!wrap)
+            continue;
+        for (int a = 0; a < 3; ++a)
+            p[a] = orc_wrap(p[a], size);
+    }
+}
+
+/* ------------------------------------------------------------------------------------
+ * Brute force: source/solvers/cpu_brute_force.h:17-43. Sequential j loop from 0, j == i
+ * skipped, FP32 accumulation acc += gravity(...).
+ * ---------------------------------------------------------------------------------- */
+typedef struct
+{
+    const float* bodies;
+    size_t n;
+    float G;
+    const int64_t* targets;
+    float* acc_out;     /* 3 per target, or NULL to write Body::acc in place */
+    float* bodies_rw;
+} orc_bf_ctx;
+
+static void orc_bf_block(void* p, const size_t begin, const size_t end)
+{
+    orc_bf_ctx* c = (orc_bf_ctx*)p;
+    for (size_t t = begin; t < end; ++t)
+    {
+        const size_t i = c->targets ? (size_t)c->targets[t] : t;
+        const float* bi = c->bodies + 12 * i;
+        float acc[3] = { 0.f, 0.f, 0.f };
+        for (size_t j = 0; j < c->n; ++j)
+        {
+            if (j == i)
+                continue;
+            const float* bj = c->bodies + 12 * j;
+            float g[3];
+            orc_gravity(bi, bi[3], bj, bj[7], c->G, g);
+            acc[0] += g[0];
+            acc[1] += g[1];
+            acc[2] += g[2];
+        }
+        if (c->acc_out)
+            memcpy(c->acc_out + 3 * t, acc, sizeof acc);
+        else
+            memcpy(c->bodies_rw + 12 * i + 8, acc, sizeof acc);
+    }
+}
+
+void orc_brute_force(float* bodies, const size_t n, const float G, const int nthreads)
+{
+    /* Results land in a side buffer first: writing Body::acc in place while other
+     * threads read the same bodies is harmless (acc is never read) but keep it simple. */
+    orc_bf_ctx c = { bodies, n, G, NULL, NULL, bodies };
+    orc_parallel(n, nthreads, orc_bf_block, &c);
+}
+
+void orc_brute_force_targets(const float* bodies, const size_t n, const float G,
+                             const int64_t* targets, const size_t ntargets, float* acc_out,
+                             const int nthreads)
+{
+    orc_bf_ctx c = { bodies, n, G, targets, acc_out, NULL };
+    orc_parallel(ntargets, nthreads, orc_bf_block, &c);
+}
+
+/* ------------------------------------------------------------------------------------
+ * Octree: source/bhtree.cpp:7-146, include/nbody/bounds.h:31-52, source/detail/tree.h.
+ * ---------------------------------------------------------------------------------- */
+struct orc_tree
+{
+    orc_node* nodes;
+    size_t count, cap;
+};
+
+static void orc_tree_push(orc_tree* t, const orc_node* n)
+{
+    if (t->count == t->cap)
+    {
+        t->cap = t->cap ? t->cap * 2 : 64;
+        t->nodes = (orc_node*)realloc(t->nodes, t->cap * sizeof(orc_node));
+    }
+    t->nodes[t->count++] = *n;
+}
+
+orc_tree* orc_tree_new(const float size)
+{
+    orc_tree* t = (orc_tree*)calloc(1, sizeof(orc_tree));
+    orc_tree_clear(t, 0.f, 0.f, 0.f, size);
+    return t;
+}
+
+void orc_tree_free(orc_tree* t)
+{
+    if (!t)
+        return;
+    free(t->nodes);
+    free(t);
+}
+
+/* Tree::clear(bounds): bhtree.cpp:140-146 -- a lone root with the new bounds. */
+void orc_tree_clear(orc_tree* t, const float cx, const float cy, const float cz, const float size)
+{
+    orc_node root;
+    memset(&root, 0, sizeof root);
+    root.cx = cx;
+    root.cy = cy;
+    root.cz = cz;
+    root.size = size;
+    t->count = 0;
+    orc_tree_push(t, &root);
+}
+
+size_t orc_tree_size(const orc_tree* t) { return t->count; }
+const orc_node* orc_tree_nodes(const orc_tree* t) { return t->nodes; }
+
+/* Bounds::quadrant: bit0 = x < cx, bit1 = y < cy, bit2 = z < cz (bounds.h:31-38). */
+static unsigned orc_quadrant(const orc_node* n, const float x, const float y, const float z)
+{
+    return (unsigned)(x < n->cx) | ((unsigned)(y < n->cy) << 1) | ((unsigned)(z < n->cz) << 2);
+}
+
+/* Tree::accumulate: running weighted mean, bhtree.cpp:87-95. */
+static void orc_accumulate(orc_node* n, const float x, const float y, const float z, const float m)
+{
+    const float nm = n->mass;
+    const float total = m + nm;
+    const float px = (x * m) + (n->comx * nm);
+    const float py = (y * m) + (n->comy * nm);
+    const float pz = (z * m) + (n->comz * nm);
+    n->mass = total;
+    n->comx = px / total;
+    n->comy = py / total;
+    n->comz = pz / total;
+}
+
+/* Tree::insert: bhtree.cpp:14-85. */
+void orc_tree_insert(orc_tree* t, const float x, const float y, const float z, const float mass)
+{
+    uint32_t idx = 0;
+    while (t->nodes[idx].children != 0)
+    {
+        orc_accumulate(&t->nodes[idx], x, y, z, mass);
+        const unsigned q = orc_quadrant(&t->nodes[idx], x, y, z);
+        idx = t->nodes[idx].children + q;
+    }
+
+    if (t->nodes[idx].mass == 0)
+    {
+        t->nodes[idx].mass = mass;
+        t->nodes[idx].comx = x;
+        t->nodes[idx].comy = y;
+        t->nodes[idx].comz = z;
+        return;
+    }
+
+    for (;;)
+    {
+        if (t->nodes[idx].size < FLT_EPSILON)
+        {
+            t->nodes[idx].mass += mass;
+            return;
+        }
+
+        /* Bounds::quadrant_bounds (bounds.h:40-52) for the 8 children, threaded so
+         * that child q's next is child q+1 and the last child's next is the parent's. */
+        const orc_node parent = t->nodes[idx];
+        const uint32_t child = (uint32_t)t->count;
+        t->nodes[idx].children = child;
+        const float half = parent.size * .5f;
+        const float quart = parent.size * .25f;
+        for (unsigned q = 0; q < 8; ++q)
+        {
+            orc_node c;
+            memset(&c, 0, sizeof c);
+            c.cx = (q & 1u) ? (parent.cx - quart) : (parent.cx + quart);
+            c.cy = (q & 2u) ? (parent.cy - quart) : (parent.cy + quart);
+            c.cz = (q & 4u) ? (parent.cz - quart) : (parent.cz + quart);
+            c.size = half;
+            c.next = (q < 7) ? (child + q + 1) : parent.next;
+            orc_tree_push(t, &c);
+        }
+
+        const unsigned new_q = orc_quadrant(&parent, x, y, z);
+        const unsigned old_q = orc_quadrant(&parent, parent.comx, parent.comy, parent.comz);
+        if (new_q == old_q)
+        {
+            const uint32_t c = t->nodes[idx].children + new_q;
+            t->nodes[c].mass = t->nodes[idx].mass;
+            t->nodes[c].comx = t->nodes[idx].comx;
+            t->nodes[c].comy = t->nodes[idx].comy;
+            t->nodes[c].comz = t->nodes[idx].comz;
+            orc_accumulate(&t->nodes[idx], x, y, z, mass);
+            idx = c;
+        }
+        else
+        {
+            const uint32_t ni = t->nodes[idx].children + new_q;
+            const uint32_t oi = t->nodes[idx].children + old_q;
+            t->nodes[ni].comx = x;
+            t->nodes[ni].comy = y;
+            t->nodes[ni].comz = z;
+            t->nodes[ni].mass = mass;
+            t->nodes[oi].comx = t->nodes[idx].comx;
+            t->nodes[oi].comy = t->nodes[idx].comy;
+            t->nodes[oi].comz = t->nodes[idx].comz;
+            t->nodes[oi].mass = t->nodes[idx].mass;
+            orc_accumulate(&t->nodes[idx], x, y, z, mass);
+            return;
+        }
+    }
+}
+
+/* detail::build_tree: tree.h:14-29 -- root centred at the origin with edge `size`,
+ * bodies inserted in index order. */
+void orc_tree_build(orc_tree* t, const float* bodies, const size_t n, const float size)
+{
+    orc_tree_clear(t, 0.f, 0.f, 0.f, size);
+    for (size_t i = 0; i < n; ++i)
+    {
+        const float* b = bodies + 12 * i;
+        orc_tree_insert(t, b[0], b[1], b[2], b[7]);
+    }
+}
+
+/* Tree::apply with the gravity visitor: bhtree.cpp:97-138 and cpu_barnes_hut.h:31-41. */
+typedef struct
+{
+    const orc_tree* tree;
+    const float* bodies;
+    const int64_t* targets;
+    float theta, G;
+    float* acc_out;
+    uint64_t* counts;   /* per target interaction counts */
+} orc_bh_ctx;
+
+static void orc_bh_block(void* p, const size_t begin, const size_t end)
+{
+    orc_bh_ctx* c = (orc_bh_ctx*)p;
+    const orc_node* nodes = c->tree->nodes;
+    const size_t count = c->tree->count;
+    const float theta_sq = c->theta * c->theta;
+    for (size_t t = begin; t < end; ++t)
+    {
+        const size_t i = c->targets ? (size_t)c->targets[t] : t;
+        const float* b = c->bodies + 12 * i;
+        float acc[3] = { 0.f, 0.f, 0.f };
+        uint64_t visits = 0;
+        uint32_t idx = 0;
+        do
+        {
+            const orc_node* nd = &nodes[idx];
+            if (nd->mass == 0)
+            {
+                idx = nd->next;
+                continue;
+            }
+            int apply = nd->children == 0;
+            if (!apply)
+            {
+                const float node_size_sq = nd->size * nd->size;
+                const float dx = nd->comx - b[0];
+                const float dy = nd->comy - b[1];
+                const float dz = nd->comz - b[2];
+                const float dist_sq = (dx * dx + dy * dy) + dz * dz;
+                apply = dist_sq > node_size_sq * theta_sq;
+            }
+            if (apply)
+            {
+                const float com[3] = { nd->comx, nd->comy, nd->comz };
+                float g[3];
+                orc_gravity(b, b[3], com, nd->mass, c->G, g);
+                acc[0] += g[0];
+                acc[1] += g[1];
+                acc[2] += g[2];
+                ++visits;
+                idx = nd->next;
+                continue;
+            }
+            idx = nd->children;
+        } while (0 < idx && idx < count);
+        memcpy(c->acc_out + 3 * t, acc, sizeof acc);
+        if (c->counts)
+            c->counts[t] = visits;
+    }
+}
+
+void orc_tree_accel(const orc_tree* t, const float* bodies, const size_t n,
+                    const int64_t* targets, const size_t ntargets, const float theta,
+                    const float G, float* acc_out, uint64_t* interactions, const int nthreads)
+{
+    const size_t nt = targets ? ntargets : n;
+    uint64_t* counts = interactions ? (uint64_t*)calloc(nt ? nt : 1, sizeof(uint64_t)) : NULL;
+    orc_bh_ctx c = { t, bodies, targets, theta, G, acc_out, counts };
+    orc_parallel(nt, nthreads, orc_bh_block, &c);
+    if (interactions)
+    {
+        uint64_t total = 0;
+        for (size_t i = 0; i < nt; ++i)
+            total += counts[i];
+        *interactions = total;
+        free(counts);
+    }
+}
+
+/* CpuBarnesHutSolver::accelerate: cpu_barnes_hut.h:22-44 (acc written in place). */
+void orc_barnes_hut(float* bodies, const size_t n, const float size, const float theta,
+                    const float G, const int nthreads, uint64_t* interactions)
+{
+    orc_tree* t = orc_tree_new(size);
+    orc_tree_build(t, bodies, n, size);
+    float* acc = (float*)malloc(sizeof(float) * 3 * (n ? n : 1));
+    orc_tree_accel(t, bodies, n, NULL, 0, theta, G, acc, interactions, nthreads);
+    for (size_t i = 0; i < n; ++i)
+        memcpy(bodies + 12 * i + 8, acc + 3 * i, 3 * sizeof(float));
+    free(acc);
+    orc_tree_free(t);
+}
+
+/* ------------------------------------------------------------------------------------
+ * FP64 direct sum with Neumaier-compensated accumulation. No reference counterpart:
+ * the checker every precision claim is stated against.
+ * ---------------------------------------------------------------------------------- */
+typedef struct { double s, c; } orc_ksum;
+
+static inline void orc_kadd(orc_ksum* k, const double v)
+{
+    const double t = k->s + v;
+    if (fabs(k->s) >= fabs(v))
+        k->c += (k->s - t) + v;
+    else
+        k->c += (v - t) + k->s;
+    k->s = t;
+}
+
+static inline double orc_kval(const orc_ksum* k) { return k->s + k->c; }
+
+typedef struct
+{
+    const float* pm;
+    const float* radius;
+    const double* pos64;
+    const double* mass64;
+    size_t n;
+    double G, eps2;
+    int law;
+    const int64_t* targets;
+    double* acc_out;
+    double* scale_out;
+} orc_f64_ctx;
+
+static void orc_f64_block(void* p, const size_t begin, const size_t end)
+{
+    orc_f64_ctx* c = (orc_f64_ctx*)p;
+    for (size_t t = begin; t < end; ++t)
+    {
+        const size_t i = c->targets ? (size_t)c->targets[t] : t;
+        double xi, yi, zi;
+        if (c->pos64)
+        {
+            xi = c->pos64[3 * i]; yi = c->pos64[3 * i + 1]; zi = c->pos64[3 * i + 2];
+        }
+        else
+        {
+            xi = c->pm[4 * i]; yi = c->pm[4 * i + 1]; zi = c->pm[4 * i + 2];
+        }
+        const double r = (c->radius && c->law == ORC_LAW_CUTOFF) ? (double)c->radius[i] : 0.0;
+        const double rsq = r * r;
+        orc_ksum ax = { 0, 0 }, ay = { 0, 0 }, az = { 0, 0 }, sc = { 0, 0 };
+        for (size_t j = 0; j < c->n; ++j)
+        {
+            double dx, dy, dz, m;
+            if (c->pos64)
+            {
+                dx = c->pos64[3 * j] - xi; dy = c->pos64[3 * j + 1] - yi; dz = c->pos64[3 * j + 2] - zi;
+                m = c->mass64[j];
+            }
+            else
+            {
+                dx = (double)c->pm[4 * j] - xi;
+                dy = (double)c->pm[4 * j + 1] - yi;
+                dz = (double)c->pm[4 * j + 2] - zi;
+                m = c->pm[4 * j + 3];
+            }
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            double f;
+            if (c->law == ORC_LAW_CUTOFF)
+            {
+                if (d2 <= rsq || d2 == 0.0)
+                    continue;
+                f = c->G * m / (sqrt(d2) * d2);
+            }
+            else
+            {
+                const double s2 = d2 + c->eps2;
+                if (s2 == 0.0)
+                    continue;
+                f = c->G * m / (sqrt(s2) * s2);
+            }
+            orc_kadd(&ax, f * dx);
+            orc_kadd(&ay, f * dy);
+            orc_kadd(&az, f * dz);
+            if (c->scale_out)
+                orc_kadd(&sc, fabs(f) * sqrt(d2));
+        }
+        c->acc_out[3 * t] = orc_kval(&ax);
+        c->acc_out[3 * t + 1] = orc_kval(&ay);
+        c->acc_out[3 * t + 2] = orc_kval(&az);
+        if (c->scale_out)
+            c->scale_out[t] = orc_kval(&sc);
+    }
+}
+
+void orc_direct_f64(const float* pos_mass, const float* radius, const size_t n, const double G,
+                    const double eps2, const int law, const int64_t* targets,
+                    const size_t ntargets, double* acc_out, double* scale_out, const int nthreads)
+{
+    orc_f64_ctx c = { pos_mass, radius, NULL, NULL, n, G, eps2, law, targets, acc_out, scale_out };
+    orc_parallel(targets ? ntargets : n, nthreads, orc_f64_block, &c);
+}
+
+void orc_direct_f64_pos(const double* pos, const double* mass, const size_t n, const double G,
+                        const double eps2, const int64_t* targets, const size_t ntargets,
+                        double* acc_out, const int nthreads)
+{
+    orc_f64_ctx c = { NULL, NULL, pos, mass, n, G, eps2, ORC_LAW_SOFTENED, targets, acc_out, NULL };
+    orc_parallel(targets ? ntargets : n, nthreads, orc_f64_block, &c);
+}
+
+typedef struct
+{
+    const double* pos;
+    const double* vel;
+    const double* mass;
+    size_t n;
+    double G, eps2;
+    int nblocks;
+    double* partial;    /* per block: kinetic, potential, px, py, pz */
+} orc_en_ctx;
+
+static void orc_en_block(void* p, const size_t begin, const size_t end)
+{
+    orc_en_ctx* c = (orc_en_ctx*)p;
+    for (size_t blk = begin; blk < end; ++blk)
+    {
+        /* Rows are dealt round-robin so the triangular loop balances across blocks. */
+        orc_ksum ke = { 0, 0 }, pe = { 0, 0 }, px = { 0, 0 }, py = { 0, 0 }, pz = { 0, 0 };
+        for (size_t i = blk; i < c->n; i += (size_t)c->nblocks)
+        {
+            const double m = c->mass[i];
+            const double* v = c->vel + 3 * i;
+            orc_kadd(&ke, 0.5 * m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+            orc_kadd(&px, m * v[0]);
+            orc_kadd(&py, m * v[1]);
+            orc_kadd(&pz, m * v[2]);
+            const double* xi = c->pos + 3 * i;
+            orc_ksum row = { 0, 0 };
+            for (size_t j = i + 1; j < c->n; ++j)
+            {
+                const double* xj = c->pos + 3 * j;
+                const double dx = xj[0] - xi[0], dy = xj[1] - xi[1], dz = xj[2] - xi[2];
+                const double s2 = dx * dx + dy * dy + dz * dz + c->eps2;
+                if (s2 > 0.0)
+                    orc_kadd(&row, c->mass[j] / sqrt(s2));
+            }
+            orc_kadd(&pe, -c->G * m * orc_kval(&row));
+        }
+        double* out = c->partial + 5 * blk;
+        out[0] = orc_kval(&ke);
+        out[1] = orc_kval(&pe);
+        out[2] = orc_kval(&px);
+        out[3] = orc_kval(&py);
+        out[4] = orc_kval(&pz);
+    }
+}
+
+void orc_energy_f64(const double* pos, const double* vel, const double* mass, const size_t n,
+                    const double G, const double eps2, double* kinetic, double* potential,
+                    double momentum[3], const int nthreads)
+{
+    const int nblocks = 64;
+    double* partial = (double*)calloc(5 * (size_t)nblocks, sizeof(double));
+    orc_en_ctx c = { pos, vel, mass, n, G, eps2, nblocks, partial };
+    orc_parallel((size_t)nblocks, nthreads, orc_en_block, &c);
+    orc_ksum s[5] = { { 0, 0 }, { 0, 0 }, { 0, 0 }, { 0, 0 }, { 0, 0 } };
+    for (int b = 0; b < nblocks; ++b)
+        for (int k = 0; k < 5; ++k)
+            orc_kadd(&s[k], partial[5 * b + k]);
+    *kinetic = orc_kval(&s[0]);
+    *potential = orc_kval(&s[1]);
+    momentum[0] = orc_kval(&s[2]);
+    momentum[1] = orc_kval(&s[3]);
+    momentum[2] = orc_kval(&s[4]);
+    free(partial);
+}
+
+/* ------------------------------------------------------------------------------------
+ * Morton codes (no reference counterpart). The quantisation rounds toward -inf in both
+ * double operations so that, for a power-of-two box whose lower corner is exact, every
+ * cell boundary compares exactly as the reference's float centre comparisons do
+ * (bounds.h:31-38): floor(rd(v)) == floor(v) whenever the boundaries are representable.
+ * ---------------------------------------------------------------------------------- */
+static uint64_t orc_spread3(uint64_t v)
+{
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x001f00000000ffffull;
+    v = (v | (v << 16)) & 0x001f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+void orc_morton63(const float* xyz, const size_t stride, const size_t n, const double lo[3],
+                  const double inv_cell, uint64_t* codes)
+{
+    const int old = fegetround();
+    fesetround(FE_DOWNWARD);
+    for (size_t i = 0; i < n; ++i)
+    {
+        uint64_t code = 0;
+        for (int a = 0; a < 3; ++a)
+        {
+            volatile double x = (double)xyz[stride * i + (size_t)a];
+            volatile double t = x - lo[a];
+            volatile double u = t * inv_cell;
+            const double f = floor(u);
+            uint64_t q;
+            if (!(f >= 0.0))
+                q = 0;
+            else if (f > 2097151.0)
+                q = 2097151;
+            else
+                q = (uint64_t)f;
+            code |= orc_spread3(q) << a;
+        }
+        codes[i] = code;
+    }
+    fesetround(old);
+}
+
+static const uint64_t* orc_sort_keys;
+
+static int orc_cmp_order(const void* a, const void* b)
+{
+    const uint32_t ia = *(const uint32_t*)a, ib = *(const uint32_t*)b;
+    const uint64_t ka = orc_sort_keys[ia], kb = orc_sort_keys[ib];
+    if (ka != kb)
+        return ka < kb ? -1 : 1;
+    return ia < ib ? -1 : (ia > ib ? 1 : 0);
+}
+
+void orc_sort_order(const uint64_t* codes, const size_t n, uint32_t* order)
+{
+    for (size_t i = 0; i < n; ++i)
+        order[i] = (uint32_t)i;
+    orc_sort_keys = codes;
+    qsort(order, n, sizeof(uint32_t), orc_cmp_order);
+    orc_sort_keys = NULL;
+}

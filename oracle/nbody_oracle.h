@@ -1,0 +1,102 @@
+/*
+ * CPU oracle for the N-body hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * This is a plain-C restatement of the reference CPU solvers (stett/nbody) plus FP64
+ * checkers that the reference lacks. It exists so the CUDA path can be checked; nothing
+ * in the product (nbody_gb300/, include/) may link or call it. Only tests/, the smoke
+ * check in __graft_entry__.py and the CPU-baseline leg of bench.py use it.
+ *
+ * Parity is pinned two ways (tests/test_oracle.py):
+ *   - against the reference's own known answers (tests/source/test_bhtree.cpp:30-142,
+ *     node counts 1/9/17 and hand-computed centres of mass), and
+ *   - bit-for-bit against the reference itself, compiled from its sources into
+ *     oracle/_ref/ by oracle/build_oracle.py, through golden fixtures in tests/golden/.
+ *
+ * Body layout (include/nbody/body.h:6-19): 12 floats per body,
+ *   [0..2] pos, [3] radius, [4..6] vel, [7] mass, [8..10] acc, [11] pad.
+ * Node layout (include/nbody/bhtree.h:13-22): 12 words per node,
+ *   center xyz, size, com xyz, mass, next, children, pad, pad.
+ */
+#ifndef NBODY_ORACLE_H
+#define NBODY_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_LAW_CUTOFF = 0, ORC_LAW_SOFTENED = 1 };
+
+typedef struct
+{
+    float cx, cy, cz, size;     /* Bounds: centre and edge */
+    float comx, comy, comz;     /* centre of mass */
+    float mass;
+    uint32_t next;              /* threaded link: next sibling or the parent's next */
+    uint32_t children;          /* first of 8 contiguous children, 0 for a leaf */
+    uint32_t pad0, pad1;
+} orc_node;
+
+typedef struct orc_tree orc_tree;
+
+/* --- force law and integrator (source/detail/physics.h) --------------------------- */
+void orc_gravity(const float pos[3], float radius, const float src[3], float src_mass,
+                 float G, float out[3]);
+float orc_wrap(float x, float size);
+void orc_integrate(float* bodies, size_t n, float dt, float size, int wrap);
+
+/* --- solvers (source/solvers/cpu_brute_force.h, cpu_barnes_hut.h) ----------------- */
+void orc_brute_force(float* bodies, size_t n, float G, int nthreads);
+/* Brute force for a subset of targets only; acc_out is 3 floats per listed target. */
+void orc_brute_force_targets(const float* bodies, size_t n, float G,
+                             const int64_t* targets, size_t ntargets, float* acc_out,
+                             int nthreads);
+void orc_barnes_hut(float* bodies, size_t n, float size, float theta, float G,
+                    int nthreads, uint64_t* interactions);
+
+/* --- octree (source/bhtree.cpp, source/detail/tree.h) ----------------------------- */
+orc_tree* orc_tree_new(float size);
+void orc_tree_free(orc_tree* t);
+void orc_tree_clear(orc_tree* t, float cx, float cy, float cz, float size);
+void orc_tree_insert(orc_tree* t, float x, float y, float z, float mass);
+void orc_tree_build(orc_tree* t, const float* bodies, size_t n, float size);
+size_t orc_tree_size(const orc_tree* t);
+const orc_node* orc_tree_nodes(const orc_tree* t);
+/* Barnes-Hut acceleration for listed targets (or all bodies when targets is NULL). */
+void orc_tree_accel(const orc_tree* t, const float* bodies, size_t n,
+                    const int64_t* targets, size_t ntargets, float theta, float G,
+                    float* acc_out, uint64_t* interactions, int nthreads);
+
+/* --- FP64 direct sum (no reference counterpart) ----------------------------------- */
+/* pos_mass: 4 floats per body (x, y, z, m). radius: per-body cutoff radius for
+ * ORC_LAW_CUTOFF (may be NULL: 0). Compensated (Neumaier) double accumulation.
+ * acc_out: 3 doubles per target; scale_out (optional): sum over j of |a_ij|. */
+void orc_direct_f64(const float* pos_mass, const float* radius, size_t n, double G,
+                    double eps2, int law, const int64_t* targets, size_t ntargets,
+                    double* acc_out, double* scale_out, int nthreads);
+/* Same law with positions given in double (for the split-precision form). */
+void orc_direct_f64_pos(const double* pos, const double* mass, size_t n, double G,
+                        double eps2, const int64_t* targets, size_t ntargets,
+                        double* acc_out, int nthreads);
+/* Kinetic and potential energy, total momentum, in double. */
+void orc_energy_f64(const double* pos, const double* vel, const double* mass, size_t n,
+                    double G, double eps2, double* kinetic, double* potential,
+                    double momentum[3], int nthreads);
+
+/* --- Morton codes and sort order (no reference counterpart) ----------------------- */
+/* Per axis q = floor((x - lo) * inv_cell) with both double operations rounded toward
+ * -inf, clamped to [0, 2^21-1]; bits interleaved x -> bit 0, y -> bit 1, z -> bit 2. */
+void orc_morton63(const float* xyz, size_t stride, size_t n, const double lo[3],
+                  double inv_cell, uint64_t* codes);
+/* Stable order by (code, index). */
+void orc_sort_order(const uint64_t* codes, size_t n, uint32_t* order);
+
+/* Threads this process would use by default (online CPUs). */
+int orc_default_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
