@@ -1,0 +1,54 @@
+"""Run one workload a fixed number of times and exit -- the target for profiler captures.
+
+    python -m nbody_gb300.run_case direct --n 262144 --steps 1
+    python -m nbody_gb300.run_case direct-aos --n 262144
+    python -m nbody_gb300.run_case integrate --n 16777216
+
+Inputs are the seeded scenes of :mod:`nbody_gb300.scenes`; nothing is timed or checked.
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+from pathlib import Path
+
+sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
+
+
+def main(argv=None) -> int:
+    from nbody_gb300 import native, scenes
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["direct", "direct-aos", "direct-cutoff", "integrate", "update",
+                                     "compensated", "fp64", "bh"])
+    ap.add_argument("--n", type=int, default=1 << 18)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--theta", type=float, default=0.5)
+    a = ap.parse_args(argv)
+
+    layout = native.LAYOUT_AOS if a.case == "direct-aos" else native.LAYOUT_SOA
+    if a.case == "bh":
+        bodies = scenes.two_plummer(a.n // 2)
+    else:
+        bodies = scenes.uniform_cube(a.n, seed=1003)
+    law = native.LAW_CUTOFF if a.case == "direct-cutoff" else native.LAW_SOFTENED
+    prec = {"compensated": native.PREC_COMPENSATED, "fp64": native.PREC_FP64}.get(a.case, native.PREC_FP32)
+    mode = native.MODE_NLOGN if a.case == "bh" else native.MODE_N2
+    p = native.params(dt=1e-3, G=1.0, eps2=1e-6, law=law, precision=prec, mode=mode, theta=a.theta,
+                      size=64.0)
+    with native.Context(layout) as ctx:
+        ctx.upload_bodies(bodies)
+        for _ in range(a.steps):
+            if a.case == "integrate":
+                ctx.integrate(p)
+            elif a.case == "update":
+                ctx.update(p, 1)
+            else:
+                ctx.accelerate(p)
+        ctx.synchronize()
+        print(f"{a.case}: n={a.n} steps={a.steps} launches={ctx.launches()}")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
