@@ -179,6 +179,24 @@ int nbody_cuda_dev_accel_aos(nbody_cuda* ctx, void* bodies, size_t n,
 int nbody_cuda_dev_integrate_soa(nbody_cuda* ctx, void* pos_mass, void* vel_radius,
                                  const void* acc, size_t n, const nbody_step_params* p);
 
+/* Direct-sum accelerate over caller-owned device buffers that allocates nothing. It has
+ * no counterpart in the reference. It is for callers that cannot let a library call
+ * cudaMalloc: a renderer or engine frame loop that must not stall on the device-wide
+ * synchronisation cudaMalloc/cudaFree imply, or a plugin whose host application owns
+ * every device allocation and its budget.
+ *
+ * Inputs, outputs and results are those of nbody_cuda_dev_accel_soa (direct sum, FP32),
+ * without a context. The scratch for the source split is a fixed 16 MiB array inside the
+ * library, which every GPU that loads the library holds until the process exits. Hence
+ * n <= 1048576; a larger n returns NBODY_ERR_INVALID. Work is queued on `stream` (a
+ * cudaStream_t; NULL is the default stream) and waited for before the call returns;
+ * NBODY_ERR_TIMEOUT reports a device-side wait that gave up. The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress); make that first
+ * call before any stream capture. All calls share the one array, so calls that overlap
+ * on the GPU (from other host threads or streams) race: the caller must serialise them. */
+int nbody_cuda_dev_accel_soa_noalloc(const void* pos_mass, const void* vel_radius, void* acc,
+                                     size_t n, const nbody_step_params* p, void* stream);
+
 /* --- introspection ------------------------------------------------------------------- */
 
 /* Kernel launches this context queued since creation (all entry points). */

@@ -30,6 +30,7 @@ EXPORTS = (
     "nbody_cuda_integrate", "nbody_cuda_update", "nbody_cuda_synchronize",
     "nbody_cuda_dev_accel_soa", "nbody_cuda_dev_accel_aos", "nbody_cuda_dev_integrate_soa",
     "nbody_cuda_launch_count", "nbody_cuda_last_direct_config", "nbody_cuda_calibrate_fp32",
+    "nbody_cuda_dev_accel_soa_noalloc",
 )
 
 
@@ -88,6 +89,7 @@ def lib() -> C.CDLL:
         "nbody_cuda_launch_count": ([vp], C.c_uint64),
         "nbody_cuda_last_direct_config": ([vp] + [C.POINTER(C.c_int)] * 5, C.c_int),
         "nbody_cuda_calibrate_fp32": ([vp, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
+        "nbody_cuda_dev_accel_soa_noalloc": ([vp, vp, vp, sz, P, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
