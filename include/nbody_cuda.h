@@ -102,7 +102,11 @@ typedef struct nbody_step_params
     int32_t mode;       /* nbody_mode */
     int32_t law;        /* nbody_law */
     int32_t precision;  /* nbody_precision */
-    int32_t reserved[3];/* zero */
+    int32_t tree_box;   /* Barnes-Hut root box: 0 = the reference's, centred at the origin
+                           with edge `size` (source/detail/tree.h:20); 1 = the smallest
+                           power-of-two cube around the bodies (FP64 bounding box).
+                           0 with size <= 0 behaves as 1. */
+    int32_t reserved[2];/* zero */
 } nbody_step_params;
 
 typedef struct nbody_cuda nbody_cuda;
@@ -196,6 +200,21 @@ int nbody_cuda_dev_integrate_soa(nbody_cuda* ctx, void* pos_mass, void* vel_radi
  * on the GPU (from other host threads or streams) race: the caller must serialise them. */
 int nbody_cuda_dev_accel_soa_noalloc(const void* pos_mass, const void* vel_radius, void* acc,
                                      size_t n, const nbody_step_params* p, void* stream);
+
+/* --- Barnes-Hut introspection ----------------------------------------------------------- */
+
+/* Statistics of the last Barnes-Hut accelerate: out[0] = force interactions (accepted
+ * cells + bodies applied), out[1] = cells visited (summed over warps), out[2] = octree
+ * cells built. Synchronous. */
+int nbody_cuda_bh_stats(nbody_cuda* ctx, uint64_t out[3]);
+
+/* Build the Barnes-Hut tree keys for the current bodies and copy back the Morton codes in
+ * sorted order (codes, n entries), the sorted body order (order: the body index at each
+ * sorted position; equal codes keep index order) and the root box (box: lower corner
+ * xyz, edge). Any output may be NULL. Synchronous. No reference counterpart: the
+ * reference inserts bodies one by one (source/bhtree.cpp:14-85). */
+int nbody_cuda_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* codes,
+                      uint32_t* order, double box[4]);
 
 /* --- introspection ------------------------------------------------------------------- */
 

@@ -1,0 +1,766 @@
+// Barnes-Hut on the device: the reference's octree (source/bhtree.cpp:14-138) rebuilt from
+// sorted 63-bit Morton codes, traversed with the reference's opening criterion.
+//
+// Pipeline per accelerate (all on the context's stream, no host round trip):
+//   1. root box: the reference's fixed box centred at the origin with edge State::size
+//      (source/detail/tree.h:20), or the smallest power-of-two cube around the FP64
+//      bounding box of the bodies (tree_box = 1);
+//   2. morton_kernel: 21 bits per axis, q = floor((x - lo) * 2^21 / edge) with both
+//      double operations rounded toward -inf, clamped, interleaved x -> bit 0. For a
+//      power-of-two box with an exact corner this puts every body in exactly the octant
+//      the reference's float centre comparisons choose (bounds.h:31-38), whose octant
+//      bit is set when the coordinate is below the centre: reference octant = digit ^ 7.
+//   3. radix_sort_pairs over (code, index): stable, so ties keep index order;
+//   4. gather_kernel: bodies into Morton order, plus FP64 prefix sums of m and m*(x - c);
+//   5. karras_kernel: binary radix tree over the sorted codes (Karras 2012), duplicates
+//      separated by index; each internal node's common-prefix length fixes its octree
+//      level floor(prefix / 3) (capped at 21, the last Morton level);
+//   6. octree nodes = binary nodes whose level exceeds their parent's (plus the root).
+//      A reference cell whose bodies all sit in one octant (a chain of single-child
+//      cells) has the same centre of mass and mass at every level of the chain, and the
+//      smallest cell of the chain is the easiest to accept, so the chain behaves exactly
+//      as its deepest cell: that is the node kept. Each node lists its <= 8 children
+//      (cells or single bodies); cells at the Morton limit (identical codes) are buckets
+//      whose bodies are applied one by one when opened;
+//   7. traverse_kernel: a warp walks the tree for 32 Morton-consecutive targets with one
+//      shared stack of (node, lane mask) entries. Every lane evaluates the reference test
+//      itself -- accept when |com - x|^2 > size^2 * theta^2 (bhtree.cpp:117-125), leaves
+//      always applied, massless nodes skipped -- and a node is opened only for the lanes
+//      that rejected it, so each target sums exactly the nodes the reference's traversal
+//      would, in a different order.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "bh.cuh"
+#include "common.cuh"
+#include "context.cuh"
+#include "scan.cuh"
+#include "sort.cuh"
+
+namespace nbg
+{
+    namespace
+    {
+        constexpr int kMortonBits = 21;
+        constexpr int kMaxLevel = 21;
+        constexpr int kTravWarps = 8;
+        constexpr int kStack = 192;
+        constexpr int kBboxBlocks = 1024;
+    }
+
+    struct BhState
+    {
+        size_t cap = 0;                 // bodies the buffers hold
+        uint64_t* keys[2] = { nullptr, nullptr };
+        uint32_t* vals[2] = { nullptr, nullptr };
+        float4* spm = nullptr;          // pos_mass in Morton order
+        float* srad = nullptr;          // target radius in Morton order
+        int2* child = nullptr;          // binary children: >= 0 internal, < 0 ~leaf
+        int* parent = nullptr;
+        int2* range = nullptr;          // [first, last] of each internal node
+        int* prefix = nullptr;          // common-prefix bits of each internal node
+        uint32_t* octflag = nullptr;
+        uint32_t* octidx = nullptr;
+        double4* psum = nullptr;        // N + 1 prefix sums
+        OctNode* nodes = nullptr;
+        void* temp = nullptr;           // sort and scan temporaries
+        size_t temp_bytes = 0;
+        BoxParams* box = nullptr;
+        double* bbox_part = nullptr;
+        unsigned long long* stats = nullptr;   // [0] interactions, [1] node visits, [2] octree nodes
+        const uint32_t* order = nullptr;       // sorted indices of the last build (keys/vals ping-pong)
+        const uint64_t* codes = nullptr;
+    };
+
+    // ------------------------------------------------------------------------------------
+    // 1. root box
+    // ------------------------------------------------------------------------------------
+    __global__ void bbox_partial_kernel(const float4* __restrict__ src, const int stride, const int n,
+                                        double* __restrict__ part)
+    {
+        double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        {
+            const float4 p = src[static_cast<size_t>(i) * stride];
+            const double v[3] = { p.x, p.y, p.z };
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+            {
+                lo[a] = fmin(lo[a], v[a]);
+                hi[a] = fmax(hi[a], v[a]);
+            }
+        }
+        __shared__ double red[6][256];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+        {
+            red[a][threadIdx.x] = lo[a];
+            red[3 + a][threadIdx.x] = hi[a];
+        }
+        __syncthreads();
+        for (int s = blockDim.x / 2; s > 0; s >>= 1)
+        {
+            if (threadIdx.x < s)
+            {
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                {
+                    red[a][threadIdx.x] = fmin(red[a][threadIdx.x], red[a][threadIdx.x + s]);
+                    red[3 + a][threadIdx.x] = fmax(red[3 + a][threadIdx.x], red[3 + a][threadIdx.x + s]);
+                }
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x < 6)
+            part[blockIdx.x * 6 + threadIdx.x] = red[threadIdx.x][0];
+    }
+
+    __global__ void box_final_kernel(const double* __restrict__ part, const int nparts, const int mode,
+                                     const float size, BoxParams* __restrict__ box)
+    {
+        if (threadIdx.x != 0 || blockIdx.x != 0)
+            return;
+        BoxParams b;
+        if (mode == 0)
+        {
+            // tree.h:20 / bhtree.h:29: centred at the origin, edge State::size
+            const double e = static_cast<double>(size);
+            for (int a = 0; a < 3; ++a)
+            {
+                b.lo[a] = -0.5 * e;
+                b.center[a] = 0.0;
+            }
+            b.edge = e;
+        }
+        else
+        {
+            double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
+            for (int k = 0; k < nparts; ++k)
+                for (int a = 0; a < 3; ++a)
+                {
+                    lo[a] = fmin(lo[a], part[k * 6 + a]);
+                    hi[a] = fmax(hi[a], part[k * 6 + 3 + a]);
+                }
+            double ext = 0.0;
+            for (int a = 0; a < 3; ++a)
+                ext = fmax(ext, hi[a] - lo[a]);
+            double e = 1.0;
+            if (ext > 0.0 && isfinite(ext))
+                e = exp2(ceil(log2(ext)));
+            if (e <= ext)
+                e *= 2.0;       // keep the maximum strictly inside the top cell
+            for (int a = 0; a < 3; ++a)
+            {
+                b.center[a] = isfinite(lo[a]) ? 0.5 * (lo[a] + hi[a]) : 0.0;
+                b.lo[a] = b.center[a] - 0.5 * e;
+            }
+            b.edge = e;
+        }
+        b.inv_cell = static_cast<double>(1u << kMortonBits) / b.edge;
+        *box = b;
+    }
+
+    // ------------------------------------------------------------------------------------
+    // 2. Morton codes
+    // ------------------------------------------------------------------------------------
+    __device__ __forceinline__ uint64_t spread3(uint64_t v)
+    {
+        v &= 0x1fffffull;
+        v = (v | (v << 32)) & 0x001f00000000ffffull;
+        v = (v | (v << 16)) & 0x001f0000ff0000ffull;
+        v = (v | (v << 8)) & 0x100f00f00f00f00full;
+        v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+        v = (v | (v << 2)) & 0x1249249249249249ull;
+        return v;
+    }
+
+    __device__ __forceinline__ uint64_t quantise(const float x, const double lo, const double inv_cell)
+    {
+        const double t = __dmul_rd(__dsub_rd(static_cast<double>(x), lo), inv_cell);
+        const double f = floor(t);
+        if (!(f >= 0.0))
+            return 0;
+        if (f > 2097151.0)
+            return 2097151;
+        return static_cast<uint64_t>(f);
+    }
+
+    __global__ void morton_kernel(const float4* __restrict__ src, const int stride, const int n,
+                                  const BoxParams* __restrict__ box, uint64_t* __restrict__ keys,
+                                  uint32_t* __restrict__ vals)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n)
+            return;
+        const float4 p = src[static_cast<size_t>(i) * stride];
+        const BoxParams b = *box;
+        keys[i] = spread3(quantise(p.x, b.lo[0], b.inv_cell)) | (spread3(quantise(p.y, b.lo[1], b.inv_cell)) << 1)
+                  | (spread3(quantise(p.z, b.lo[2], b.inv_cell)) << 2);
+        vals[i] = static_cast<uint32_t>(i);
+    }
+
+    // ------------------------------------------------------------------------------------
+    // 4. Morton-ordered copies and FP64 prefix-sum inputs
+    // ------------------------------------------------------------------------------------
+    __global__ void gather_kernel(const float4* __restrict__ src, const int stride,
+                                  const float4* __restrict__ vel_radius, const uint32_t* __restrict__ order,
+                                  const int n, const BoxParams* __restrict__ box, float4* __restrict__ spm,
+                                  float* __restrict__ srad, double4* __restrict__ psum)
+    {
+        const int k = blockIdx.x * blockDim.x + threadIdx.x;
+        if (k > n)
+            return;
+        if (k == n)
+        {
+            psum[n] = make_double4(0, 0, 0, 0);
+            return;
+        }
+        const uint32_t i = order[k];
+        const float4 p = src[static_cast<size_t>(i) * stride];
+        float m, r;
+        if (stride == 3)
+        {
+            m = src[static_cast<size_t>(i) * 3 + 1].w;    // Body: {pos, radius}, {vel, mass}
+            r = p.w;
+        }
+        else
+        {
+            m = p.w;
+            r = vel_radius ? vel_radius[i].w : 0.f;
+        }
+        spm[k] = make_float4(p.x, p.y, p.z, m);
+        srad[k] = r;
+        const double dm = m;
+        psum[k] = make_double4(dm * (static_cast<double>(p.x) - box->center[0]),
+                               dm * (static_cast<double>(p.y) - box->center[1]),
+                               dm * (static_cast<double>(p.z) - box->center[2]), dm);
+    }
+
+    // ------------------------------------------------------------------------------------
+    // 5. binary radix tree (Karras 2012)
+    // ------------------------------------------------------------------------------------
+    __device__ __forceinline__ int delta(const uint64_t* __restrict__ keys, const int n, const int i, const int j)
+    {
+        if (j < 0 || j >= n)
+            return -1;
+        const uint64_t a = keys[i], b = keys[j];
+        if (a != b)
+            return __clzll(static_cast<long long>(a ^ b));
+        return 64 + __clz(static_cast<int>(static_cast<unsigned>(i) ^ static_cast<unsigned>(j)));
+    }
+
+    __global__ void karras_kernel(const uint64_t* __restrict__ keys, const int n, int2* __restrict__ child,
+                                  int* __restrict__ parent, int2* __restrict__ range, int* __restrict__ prefix)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n - 1)
+            return;
+        const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+        const int dmin = delta(keys, n, i, i - d);
+        int lmax = 2;
+        while (delta(keys, n, i, i + lmax * d) > dmin)
+            lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (delta(keys, n, i, i + (l + t) * d) > dmin)
+                l += t;
+        const int j = i + l * d;
+        const int dnode = delta(keys, n, i, j);
+        int s = 0;
+        for (int t = (l + 1) >> 1;; t = (t + 1) >> 1)
+        {
+            if (delta(keys, n, i, i + (s + t) * d) > dnode)
+                s += t;
+            if (t == 1)
+                break;
+        }
+        const int gamma = i + s * d + min(d, 0);
+        const int lo = min(i, j), hi = max(i, j);
+        const int left = (lo == gamma) ? ~gamma : gamma;
+        const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+        child[i] = make_int2(left, right);
+        range[i] = make_int2(lo, hi);
+        prefix[i] = dnode - 1;     // codes are 63-bit: the top key bit is always shared
+        if (left >= 0)
+            parent[left] = i;
+        if (right >= 0)
+            parent[right] = i;
+        if (i == 0)
+            parent[0] = -1;
+    }
+
+    __device__ __forceinline__ int level_of(const int prefix) { return min(kMaxLevel, prefix / 3); }
+
+    __global__ void octflag_kernel(const int* __restrict__ parent, const int* __restrict__ prefix, const int m,
+                                   uint32_t* __restrict__ flag)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= m)
+            return;
+        const int p = parent[i];
+        flag[i] = (i == 0 || p < 0 || level_of(prefix[i]) > level_of(prefix[p])) ? 1u : 0u;
+    }
+
+    // ------------------------------------------------------------------------------------
+    // 6. octree records
+    // ------------------------------------------------------------------------------------
+    __global__ void octnode_kernel(const int2* __restrict__ child, const int2* __restrict__ range,
+                                   const int* __restrict__ prefix, const uint32_t* __restrict__ flag,
+                                   const uint32_t* __restrict__ octidx, const double4* __restrict__ psum,
+                                   const int m, const BoxParams* __restrict__ box, const float theta,
+                                   OctNode* __restrict__ nodes, unsigned* __restrict__ err,
+                                   unsigned long long* __restrict__ stats)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= m || !flag[i])
+            return;
+        const int2 rg = range[i];
+        const int lvl = level_of(prefix[i]);
+        const double4 hi = psum[rg.y + 1], lo = psum[rg.x];
+        const double ms = hi.w - lo.w;
+        OctNode nd;
+        const BoxParams b = *box;
+        if (ms > 0.0)
+        {
+            nd.com_mass = make_float4(static_cast<float>(b.center[0] + (hi.x - lo.x) / ms),
+                                      static_cast<float>(b.center[1] + (hi.y - lo.y) / ms),
+                                      static_cast<float>(b.center[2] + (hi.z - lo.z) / ms), static_cast<float>(ms));
+        }
+        else
+            nd.com_mass = make_float4(0.f, 0.f, 0.f, 0.f);
+        // the reference's node size is the root size halved per level, in float
+        const float s = static_cast<float>(ldexp(b.edge, -lvl));
+        const float size_sq = __fmul_rn(s, s);
+        nd.open_r2 = __fmul_rn(size_sq, __fmul_rn(theta, theta));
+        nd.first = rg.x;
+        nd.last = rg.y;
+        for (int c = 0; c < 8; ++c)
+            nd.child[c] = 0;
+        if (prefix[i] >= 3 * kMaxLevel)
+            nd.nchild = -1;     // bucket: identical codes, bodies applied one by one
+        else
+        {
+            // Walk down through the binary nodes of the same level (at most 7 below a cell
+            // with 8 children) collecting the next cells and single bodies.
+            int stack[8];
+            int sp = 0, nc = 0;
+            stack[sp++] = child[i].x;
+            stack[sp++] = child[i].y;
+            while (sp > 0)
+            {
+                const int c = stack[--sp];
+                if (c < 0 || flag[c])
+                {
+                    if (nc < 8)
+                        nd.child[nc] = c < 0 ? c : static_cast<int>(octidx[c]);
+                    else
+                        atomicOr(err, DEV_ERR_BOUNDS);
+                    ++nc;
+                }
+                else if (sp + 2 <= 8)
+                {
+                    stack[sp++] = child[c].x;
+                    stack[sp++] = child[c].y;
+                }
+                else
+                    atomicOr(err, DEV_ERR_BOUNDS);
+            }
+            nd.nchild = min(nc, 8);
+        }
+        nodes[octidx[i]] = nd;
+        if (i == 0)
+            atomicAdd(&stats[2], static_cast<unsigned long long>(octidx[m - 1] + flag[m - 1]));
+    }
+
+    // ------------------------------------------------------------------------------------
+    // 7. traversal
+    // ------------------------------------------------------------------------------------
+    template <int LAW>
+    __device__ __forceinline__ void apply(const float px, const float py, const float pz, const float lim,
+                                          const float sx, const float sy, const float sz, const float m,
+                                          float& ax, float& ay, float& az)
+    {
+        const float dx = sx - px, dy = sy - py, dz = sz - pz;
+        float r2 = (LAW == NBODY_LAW_SOFTENED) ? fmaf(dx, dx, lim) : dx * dx;
+        r2 = fmaf(dy, dy, r2);
+        r2 = fmaf(dz, dz, r2);
+        float inv = rsqrt_sfu(r2);
+        if (LAW == NBODY_LAW_CUTOFF)
+            inv = r2 > lim ? inv : 0.f;     // physics.h:38-39
+        const float s = m * inv * inv * inv;
+        ax = fmaf(dx, s, ax);
+        ay = fmaf(dy, s, ay);
+        az = fmaf(dz, s, az);
+    }
+
+    template <int LAW>
+    __global__ void __launch_bounds__(kTravWarps * 32) traverse_kernel(
+        const OctNode* __restrict__ nodes, const float4* __restrict__ spm, const float* __restrict__ srad,
+        const uint32_t* __restrict__ order, const int n, const float G, const float eps2,
+        float4* __restrict__ acc, float* __restrict__ body_out, unsigned* __restrict__ err,
+        unsigned long long* __restrict__ stats)
+    {
+        __shared__ int stk_node[kTravWarps][kStack];
+        __shared__ unsigned stk_mask[kTravWarps][kStack];
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const unsigned lt = (1u << lane) - 1u;
+        unsigned long long inter = 0, visits = 0;
+
+        for (int tile = blockIdx.x * kTravWarps + warp; tile * 32 < n; tile += gridDim.x * kTravWarps)
+        {
+            const int k = tile * 32 + lane;
+            const bool valid = k < n;
+            const float4 me = spm[valid ? k : n - 1];
+            const float rad = srad[valid ? k : n - 1];
+            const float lim = (LAW == NBODY_LAW_CUTOFF) ? rad * rad : eps2;
+            float ax = 0.f, ay = 0.f, az = 0.f;
+            const unsigned valid_mask = __ballot_sync(0xffffffffu, valid);
+            if (lane == 0)
+            {
+                stk_node[warp][0] = 0;
+                stk_mask[warp][0] = valid_mask;
+            }
+            int sp = 1;
+            __syncwarp();
+            // Each cell is reached from its one parent, so a warp pops at most one entry
+            // per cell (< n). The bound only trips on a malformed tree: it records the
+            // error and stops this warp instead of spinning.
+            long long guard = 0;
+            while (sp > 0)
+            {
+                if (++guard > static_cast<long long>(n) + 64)
+                {
+                    if (lane == 0)
+                        atomicOr(err, DEV_ERR_BOUNDS);
+                    break;
+                }
+                --sp;
+                const int nd = stk_node[warp][sp];
+                const unsigned mask = stk_mask[warp][sp];
+                __syncwarp();
+                ++visits;
+                const float4 cm = nodes[nd].com_mass;
+                if (cm.w == 0.f)
+                    continue;       // bhtree.cpp:109-113: empty nodes are skipped
+                const bool in = (mask >> lane) & 1u;
+                // bhtree.cpp:117-125, evaluated in the reference's operation order
+                const float dx = __fsub_rn(cm.x, me.x), dy = __fsub_rn(cm.y, me.y), dz = __fsub_rn(cm.z, me.z);
+                const float dist_sq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                const bool accept = in && dist_sq > nodes[nd].open_r2;
+                if (accept)
+                {
+                    apply<LAW>(me.x, me.y, me.z, lim, cm.x, cm.y, cm.z, cm.w, ax, ay, az);
+                    ++inter;
+                }
+                const unsigned open = mask & ~__ballot_sync(0xffffffffu, accept);
+                if (!open)
+                    continue;
+                const bool mine = (open >> lane) & 1u;
+                const int nchild = nodes[nd].nchild;
+                if (nchild < 0)
+                {
+                    const int first = nodes[nd].first, last = nodes[nd].last;
+                    for (int b = first; b <= last; ++b)
+                    {
+                        const float4 s = spm[b];
+                        if (mine)
+                        {
+                            apply<LAW>(me.x, me.y, me.z, lim, s.x, s.y, s.z, s.w, ax, ay, az);
+                            ++inter;
+                        }
+                    }
+                    continue;
+                }
+                const int c = lane < nchild ? nodes[nd].child[lane] : 0;
+                const bool is_cell = lane < nchild && c >= 0;
+                const bool is_leaf = lane < nchild && c < 0;
+                const unsigned cells = __ballot_sync(0xffffffffu, is_cell);
+                unsigned leaves = __ballot_sync(0xffffffffu, is_leaf);
+                if (is_cell)
+                {
+                    const int at = sp + __popc(cells & lt);
+                    if (at < kStack)
+                    {
+                        stk_node[warp][at] = c;
+                        stk_mask[warp][at] = open;
+                    }
+                    else
+                        atomicOr(err, DEV_ERR_BOUNDS);
+                }
+                sp = min(kStack, sp + __popc(cells));
+                __syncwarp();
+                while (leaves)
+                {
+                    const int l = __ffs(leaves) - 1;
+                    leaves &= leaves - 1;
+                    const int b = ~__shfl_sync(0xffffffffu, c, l);
+                    const float4 s = spm[b];
+                    if (mine && s.w != 0.f)
+                    {
+                        apply<LAW>(me.x, me.y, me.z, lim, s.x, s.y, s.z, s.w, ax, ay, az);
+                        ++inter;
+                    }
+                }
+            }
+            if (valid)
+            {
+                const uint32_t i = order[k];
+                if (body_out)
+                {
+                    float* o = body_out + static_cast<size_t>(i) * 12 + 8;
+                    o[0] = G * ax;
+                    o[1] = G * ay;
+                    o[2] = G * az;
+                }
+                else
+                    acc[i] = make_float4(G * ax, G * ay, G * az, 0.f);
+            }
+        }
+        // per-warp totals
+        for (int o = 16; o > 0; o >>= 1)
+            inter += __shfl_down_sync(0xffffffffu, inter, o);
+        if (lane == 0)
+        {
+            atomicAdd(&stats[0], inter);
+            atomicAdd(&stats[1], visits);
+        }
+    }
+
+    // ------------------------------------------------------------------------------------
+    // host side
+    // ------------------------------------------------------------------------------------
+    namespace
+    {
+        template <typename T>
+        cudaError_t grow(T** p, const size_t count, cudaStream_t s)
+        {
+            if (*p)
+                cudaFreeAsync(*p, s);
+            *p = nullptr;
+            return cudaMallocAsync(reinterpret_cast<void**>(p), std::max<size_t>(count, 1) * sizeof(T), s);
+        }
+
+        int reserve_bh(nbody_cuda* ctx, const size_t n)
+        {
+            if (!ctx->bh)
+                ctx->bh = new BhState();
+            BhState& b = *ctx->bh;
+            if (!b.box)
+            {
+                cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&b.box), sizeof(BoxParams), ctx->stream);
+                if (e == cudaSuccess)
+                    e = cudaMallocAsync(reinterpret_cast<void**>(&b.bbox_part), kBboxBlocks * 6 * sizeof(double), ctx->stream);
+                if (e == cudaSuccess)
+                    e = cudaMallocAsync(reinterpret_cast<void**>(&b.stats), 4 * sizeof(unsigned long long), ctx->stream);
+                if (e != cudaSuccess)
+                    return ctx_cuda_fail(ctx, e, "tree allocation");
+            }
+            if (n <= b.cap)
+                return NBODY_OK;
+            const size_t cap = std::max(n, b.cap + b.cap / 2);
+            const size_t tb = std::max(sort_temp_bytes(cap), scan_temp_elems(cap + 1) * sizeof(double4));
+            cudaError_t e = cudaSuccess;
+            cudaStream_t s = ctx->stream;
+            for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+            {
+                e = grow(&b.keys[k], cap, s);
+                if (e == cudaSuccess)
+                    e = grow(&b.vals[k], cap, s);
+            }
+            if (e == cudaSuccess) e = grow(&b.spm, cap, s);
+            if (e == cudaSuccess) e = grow(&b.srad, cap, s);
+            if (e == cudaSuccess) e = grow(&b.child, cap, s);
+            if (e == cudaSuccess) e = grow(&b.parent, cap, s);
+            if (e == cudaSuccess) e = grow(&b.range, cap, s);
+            if (e == cudaSuccess) e = grow(&b.prefix, cap, s);
+            if (e == cudaSuccess) e = grow(&b.octflag, cap, s);
+            if (e == cudaSuccess) e = grow(&b.octidx, cap, s);
+            if (e == cudaSuccess) e = grow(&b.psum, cap + 1, s);
+            if (e == cudaSuccess) e = grow(&b.nodes, cap, s);
+            if (e == cudaSuccess)
+            {
+                if (b.temp)
+                    cudaFreeAsync(b.temp, s);
+                b.temp = nullptr;
+                e = cudaMallocAsync(&b.temp, tb, s);
+                b.temp_bytes = tb;
+            }
+            if (e != cudaSuccess)
+            {
+                b.cap = 0;
+                return ctx_cuda_fail(ctx, e, "tree allocation");
+            }
+            b.cap = cap;
+            return NBODY_OK;
+        }
+
+        const float4* body_src(const nbody_cuda* ctx, int* stride)
+        {
+            if (ctx->layout == NBODY_LAYOUT_AOS)
+            {
+                *stride = 3;
+                return reinterpret_cast<const float4*>(ctx->bodies);
+            }
+            *stride = 1;
+            return ctx->pm;
+        }
+    }
+
+    int bh_build(nbody_cuda* ctx, const nbody_step_params* p)
+    {
+        const size_t n = ctx->count;
+        if (const int st = reserve_bh(ctx, n))
+            return st;
+        BhState& b = *ctx->bh;
+        cudaStream_t s = ctx->stream;
+        int stride = 1;
+        const float4* src = body_src(ctx, &stride);
+        const int ni = static_cast<int>(n);
+        const unsigned blocks = ceil_div(n, 256);
+        uint64_t& L = ctx->launches;
+
+        cudaMemsetAsync(b.stats, 0, 4 * sizeof(unsigned long long), s);
+        // tree_box = 0 is the reference's fixed root box; it needs a positive size
+        const bool auto_box = p->tree_box != 0 || !(p->size > 0.f);
+        if (auto_box)
+        {
+            bbox_partial_kernel<<<kBboxBlocks, 256, 0, s>>>(src, stride, ni, b.bbox_part);
+            ++L;
+        }
+        box_final_kernel<<<1, 32, 0, s>>>(b.bbox_part, auto_box ? kBboxBlocks : 0, auto_box ? 1 : 0, p->size, b.box);
+        ++L;
+        morton_kernel<<<blocks, 256, 0, s>>>(src, stride, ni, b.box, b.keys[0], b.vals[0]);
+        ++L;
+        bool in_alt = false;
+        cudaError_t e = radix_sort_pairs(b.keys[0], b.vals[0], b.keys[1], b.vals[1], n, 0, 63, b.temp, s, &L, &in_alt);
+        if (e != cudaSuccess)
+            return ctx_cuda_fail(ctx, e, "radix sort");
+        const uint64_t* keys = b.keys[in_alt ? 1 : 0];
+        const uint32_t* order = b.vals[in_alt ? 1 : 0];
+        b.order = order;
+        b.codes = keys;
+        gather_kernel<<<ceil_div(n + 1, 256), 256, 0, s>>>(src, stride, ctx->layout == NBODY_LAYOUT_AOS ? nullptr : ctx->vr,
+                                                            order, ni, b.box, b.spm, b.srad, b.psum);
+        ++L;
+        e = exclusive_scan<double4>(b.psum, b.psum, n + 1, static_cast<double4*>(b.temp), s, &L);
+        if (e != cudaSuccess)
+            return ctx_cuda_fail(ctx, e, "prefix sums");
+        if (n < 2)
+            return NBODY_OK;
+        const int m = ni - 1;
+        karras_kernel<<<ceil_div(m, 256), 256, 0, s>>>(keys, ni, b.child, b.parent, b.range, b.prefix);
+        ++L;
+        octflag_kernel<<<ceil_div(m, 256), 256, 0, s>>>(b.parent, b.prefix, m, b.octflag);
+        ++L;
+        e = exclusive_scan<uint32_t>(b.octflag, b.octidx, m, static_cast<uint32_t*>(b.temp), s, &L);
+        if (e != cudaSuccess)
+            return ctx_cuda_fail(ctx, e, "octree compaction");
+        octnode_kernel<<<ceil_div(m, 256), 256, 0, s>>>(b.child, b.range, b.prefix, b.octflag, b.octidx, b.psum, m, b.box,
+                                                         p->theta, b.nodes, ctx->dev_error, b.stats);
+        ++L;
+        e = cudaGetLastError();
+        if (e != cudaSuccess)
+            return ctx_cuda_fail(ctx, e, "tree build");
+        return NBODY_OK;
+    }
+
+    int bh_accelerate(nbody_cuda* ctx, const nbody_step_params* p)
+    {
+        const size_t n = ctx->count;
+        if (const int st = bh_build(ctx, p))
+            return st;
+        BhState& b = *ctx->bh;
+        cudaStream_t s = ctx->stream;
+        const int ni = static_cast<int>(n);
+        float4* acc = ctx->layout == NBODY_LAYOUT_AOS ? nullptr : ctx->acc;
+        float* body_out = ctx->layout == NBODY_LAYOUT_AOS ? ctx->bodies : nullptr;
+        if (n < 2)
+        {
+            // a lone body feels nothing (its own leaf is cut off / multiplied by d = 0)
+            if (acc)
+                cudaMemsetAsync(acc, 0, n * sizeof(float4), s);
+            else
+                for (size_t i = 0; i < n; ++i)
+                    cudaMemsetAsync(body_out + i * 12 + 8, 0, 3 * sizeof(float), s);
+            return NBODY_OK;
+        }
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        const int tiles = (ni + 31) / 32;
+        const int grid = std::min((tiles + kTravWarps - 1) / kTravWarps, sms * 8);
+        if (p->law == NBODY_LAW_SOFTENED)
+            traverse_kernel<NBODY_LAW_SOFTENED><<<grid, kTravWarps * 32, 0, s>>>(
+                b.nodes, b.spm, b.srad, b.order, ni, p->G, p->eps2, acc, body_out, ctx->dev_error, b.stats);
+        else
+            traverse_kernel<NBODY_LAW_CUTOFF><<<grid, kTravWarps * 32, 0, s>>>(
+                b.nodes, b.spm, b.srad, b.order, ni, p->G, p->eps2, acc, body_out, ctx->dev_error, b.stats);
+        ++ctx->launches;
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess)
+            return ctx_cuda_fail(ctx, e, "tree traversal");
+        return NBODY_OK;
+    }
+
+    void release_bh(nbody_cuda* ctx)
+    {
+        if (!ctx->bh)
+            return;
+        BhState& b = *ctx->bh;
+        for (int k = 0; k < 2; ++k)
+        {
+            cudaFree(b.keys[k]);
+            cudaFree(b.vals[k]);
+        }
+        void* ptrs[] = { b.spm, b.srad, b.child, b.parent, b.range, b.prefix, b.octflag, b.octidx, b.psum,
+                         b.nodes, b.temp, b.box, b.bbox_part, b.stats };
+        for (void* q : ptrs)
+            cudaFree(q);
+        delete ctx->bh;
+        ctx->bh = nullptr;
+    }
+
+    int bh_stats(nbody_cuda* ctx, unsigned long long out[3])
+    {
+        if (!ctx->bh || !ctx->bh->stats)
+        {
+            out[0] = out[1] = out[2] = 0;
+            return NBODY_OK;
+        }
+        const cudaError_t e = cudaMemcpyAsync(out, ctx->bh->stats, 3 * sizeof(unsigned long long),
+                                              cudaMemcpyDeviceToHost, ctx->stream);
+        if (e != cudaSuccess)
+            return ctx_cuda_fail(ctx, e, "tree statistics readback");
+        return check_device_error(ctx);
+    }
+
+    int bh_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* codes, uint32_t* order, double box[4])
+    {
+        if (!ctx->count)
+            return NBODY_OK;
+        if (const int st = bh_build(ctx, p))
+            return st;
+        BhState& b = *ctx->bh;
+        const size_t n = ctx->count;
+        cudaError_t e = cudaSuccess;
+        if (codes)
+            e = cudaMemcpyAsync(codes, b.codes, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess && order)
+            e = cudaMemcpyAsync(order, b.order, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
+        BoxParams hb;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&hb, b.box, sizeof hb, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e != cudaSuccess)
+            return ctx_cuda_fail(ctx, e, "Morton readback");
+        if (const int st = check_device_error(ctx))
+            return st;
+        if (box)
+        {
+            box[0] = hb.lo[0];
+            box[1] = hb.lo[1];
+            box[2] = hb.lo[2];
+            box[3] = hb.edge;
+        }
+        return NBODY_OK;
+    }
+}

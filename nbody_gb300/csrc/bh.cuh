@@ -1,0 +1,36 @@
+// Internal interface of the Barnes-Hut pipeline (bh.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "nbody_cuda.h"
+
+struct nbody_cuda;
+
+namespace nbg
+{
+    // Root box of the Morton grid, kept on the device between the build kernels.
+    struct BoxParams
+    {
+        double lo[3];       // lower corner
+        double center[3];   // centre (prefix sums are taken relative to it)
+        double edge;        // cube edge
+        double inv_cell;    // 2^21 / edge
+    };
+
+    // One octree cell: 64 bytes, read whole by a warp (a broadcast load per field).
+    struct __align__(16) OctNode
+    {
+        float4 com_mass;    // centre of mass (float) and mass
+        float open_r2;      // (cell edge)^2 * theta^2: accepted when |com - x|^2 > open_r2
+        int nchild;         // children listed below; -1 for a bucket of identical codes
+        int first, last;    // sorted body range of the cell
+        int child[8];       // >= 0: octree cell index; < 0: ~(sorted body index)
+    };
+    static_assert(sizeof(OctNode) == 64, "OctNode is one 64-byte record");
+
+    int bh_build(nbody_cuda* ctx, const nbody_step_params* p);
+    int bh_stats(nbody_cuda* ctx, unsigned long long out[3]);
+    int bh_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* codes, uint32_t* order, double box[4]);
+}

@@ -13,6 +13,7 @@
 #include <new>
 #include <string>
 
+#include "bh.cuh"
 #include "common.cuh"
 #include "context.cuh"
 #include "direct.cuh"
@@ -629,6 +630,28 @@ int nbody_cuda_update(nbody_cuda* ctx, const nbody_step_params* p, const int ste
             return st;
     }
     return NBODY_OK;
+}
+
+// --- Barnes-Hut introspection ----------------------------------------------------------------
+
+int nbody_cuda_bh_stats(nbody_cuda* ctx, uint64_t out[3])
+{
+    if (!ctx || !out)
+        return NBODY_ERR_INVALID;
+    unsigned long long v[3];
+    const int st = bh_stats(ctx, v);
+    for (int k = 0; k < 3; ++k)
+        out[k] = v[k];
+    return st;
+}
+
+int nbody_cuda_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* codes, uint32_t* order, double box[4])
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    return bh_morton(ctx, p, codes, order, box);
 }
 
 // --- caller-owned device buffers -----------------------------------------------------------

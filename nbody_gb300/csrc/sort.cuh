@@ -1,0 +1,19 @@
+// Stable LSD radix sort of (uint64 key, uint32 value) pairs (sort.cu).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <utility>
+#include <cuda_runtime.h>
+
+namespace nbg
+{
+    // Temporary bytes radix_sort_pairs needs for n pairs.
+    size_t sort_temp_bytes(size_t n);
+
+    // Sort by bits [begin_bit, end_bit) of the key, 8 bits per pass, ping-ponging between
+    // (keys, vals) and (keys_alt, vals_alt). *in_alt tells which pair holds the result.
+    cudaError_t radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt,
+                                 size_t n, int begin_bit, int end_bit, void* temp, cudaStream_t stream,
+                                 uint64_t* launches, bool* in_alt);
+}

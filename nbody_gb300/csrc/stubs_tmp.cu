@@ -4,6 +4,4 @@ int precise_accelerate(nbody_cuda* ctx, const nbody_step_params*) { return ctx_f
 int precise_integrate(nbody_cuda* ctx, const nbody_step_params*) { return ctx_fail(ctx, NBODY_ERR_UNSUPPORTED, "compensated precision not built yet"); }
 int sync_precise_positions(nbody_cuda*) { return NBODY_OK; }
 void release_precise(nbody_cuda*) {}
-int bh_accelerate(nbody_cuda* ctx, const nbody_step_params*) { return ctx_fail(ctx, NBODY_ERR_UNSUPPORTED, "Barnes-Hut not built yet"); }
-void release_bh(nbody_cuda*) {}
 }

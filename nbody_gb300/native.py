@@ -30,7 +30,7 @@ EXPORTS = (
     "nbody_cuda_integrate", "nbody_cuda_update", "nbody_cuda_synchronize",
     "nbody_cuda_dev_accel_soa", "nbody_cuda_dev_accel_aos", "nbody_cuda_dev_integrate_soa",
     "nbody_cuda_launch_count", "nbody_cuda_last_direct_config", "nbody_cuda_calibrate_fp32",
-    "nbody_cuda_dev_accel_soa_noalloc",
+    "nbody_cuda_dev_accel_soa_noalloc", "nbody_cuda_bh_stats", "nbody_cuda_morton",
 )
 
 
@@ -38,12 +38,12 @@ class StepParams(C.Structure):
     """nbody_step_params."""
     _fields_ = [("dt", C.c_float), ("theta", C.c_float), ("G", C.c_float), ("eps2", C.c_float),
                 ("size", C.c_float), ("wrap", C.c_int32), ("mode", C.c_int32), ("law", C.c_int32),
-                ("precision", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("precision", C.c_int32), ("tree_box", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 def params(dt=0.0, theta=0.5, G=1.0, eps2=0.0, size=10000.0, wrap=False, mode=MODE_N2,
-           law=LAW_CUTOFF, precision=PREC_FP32) -> StepParams:
-    return StepParams(dt, theta, G, eps2, size, int(bool(wrap)), mode, law, precision)
+           law=LAW_CUTOFF, precision=PREC_FP32, tree_box=0) -> StepParams:
+    return StepParams(dt, theta, G, eps2, size, int(bool(wrap)), mode, law, precision, tree_box)
 
 
 class NbodyError(RuntimeError):
@@ -90,6 +90,8 @@ def lib() -> C.CDLL:
         "nbody_cuda_last_direct_config": ([vp] + [C.POINTER(C.c_int)] * 5, C.c_int),
         "nbody_cuda_calibrate_fp32": ([vp, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
         "nbody_cuda_dev_accel_soa_noalloc": ([vp, vp, vp, sz, P, vp], C.c_int),
+        "nbody_cuda_bh_stats": ([vp, C.POINTER(C.c_uint64)], C.c_int),
+        "nbody_cuda_morton": ([vp, P, vp, vp, C.POINTER(C.c_double)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -206,6 +208,19 @@ class Context:
     # --- introspection -------------------------------------------------------------------------
     def launches(self) -> int:
         return int(lib().nbody_cuda_launch_count(self.h))
+
+    def bh_stats(self) -> dict:
+        out = (C.c_uint64 * 3)()
+        self.check(lib().nbody_cuda_bh_stats(self.h, out))
+        return {"interactions": int(out[0]), "visits": int(out[1]), "cells": int(out[2])}
+
+    def morton(self, p: StepParams):
+        n = self.count()
+        codes = np.zeros(n, np.uint64)
+        order = np.zeros(n, np.uint32)
+        box = (C.c_double * 4)()
+        self.check(lib().nbody_cuda_morton(self.h, C.byref(p), _ptr(codes), _ptr(order), box))
+        return codes, order, np.array(box[:])
 
     def calibrate_fp32(self) -> tuple[float, float]:
         s, p = C.c_double(), C.c_double()

@@ -1,0 +1,216 @@
+"""Barnes-Hut on the GPU against the reference's CPU octree solver, through the C ABI.
+
+Bars:
+  * Morton codes and sort order: bit-exact against the oracle (oracle/nbody_oracle.c).
+  * Accelerations: the device tree has the reference's cells and applies the reference's
+    opening test per target, so a body's sum covers the same cells; only the centre-of-mass
+    rounding (FP64 sums here, an FP32 running mean in the reference, bhtree.cpp:87-95) and
+    the summation order differ. Per body |a_gpu - a_ref| <= 5e-5 * sum|terms| for all but
+    a handful of bodies (where a rounding difference flips one borderline acceptance), and
+    every body within the reference's own bound: max relative error < 1e-2
+    (tests/source/test_gpu.cpp:226-254).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 5e-5
+
+
+def bh_accel(native, bodies, layout=0, **kw):
+    kw.setdefault("mode", native.MODE_NLOGN)
+    with native.Context(layout) as ctx:
+        ctx.upload_bodies(bodies)
+        ctx.accelerate(native.params(**kw))
+        out = ctx.download_bodies()
+        stats = ctx.bh_stats()
+    return out[:, 8:11], stats
+
+
+def term_scale(bodies, targets=None):
+    """sum_j |a_ij| over all bodies (FP64): the natural scale of an FP32 sum's rounding."""
+    _, scale = O.direct_f64(bodies[:, [0, 1, 2, 7]], 1.0, 0.0, O.LAW_CUTOFF, radius=bodies[:, 3],
+                            targets=targets, with_scale=True)
+    return np.maximum(scale, 1e-30)
+
+
+def compare_to_reference(acc, ref, bodies, allowed_outliers):
+    err = np.linalg.norm(acc.astype(np.float64) - ref, axis=1) / term_scale(bodies)
+    bad = np.flatnonzero(err > TOL)
+    assert len(bad) <= allowed_outliers, (len(bad), err.max())
+    mag = np.linalg.norm(ref, axis=1)
+    ok = mag > 0
+    rel = np.linalg.norm(acc[ok] - ref[ok], axis=1) / mag[ok]
+    assert rel.max() < 1e-2, rel.max()
+    return err
+
+
+@pytest.mark.parametrize("layout", [0, 1], ids=["soa", "aos"])
+@pytest.mark.parametrize("fixture", ["disk_1024.npz", "disk_2048.npz", "cube_4096.npz"])
+def test_bh_matches_reference_cpu_barnes_hut(gpu, fixture, layout):
+    g = golden(fixture)
+    b = g["bodies"]
+    acc, stats = bh_accel(gpu, b, layout, theta=0.5, size=10000.0, law=gpu.LAW_CUTOFF)
+    compare_to_reference(acc, g["bh_acc"].astype(np.float64), b, allowed_outliers=max(2, len(b) // 500))
+    # the same cells are accepted, so the interaction count matches the reference's
+    t = O.Tree(10000.0)
+    t.build(b, 10000.0)
+    _, inter = t.accel(b, 0.5, 1.0)
+    assert abs(stats["interactions"] - inter) <= 0.01 * inter, (stats, inter)
+
+
+def test_bh_soa_aos_identical(gpu):
+    b = golden("cube_4096.npz")["bodies"]
+    a, _ = bh_accel(gpu, b, 0, theta=0.5, size=10000.0)
+    c, _ = bh_accel(gpu, b, 1, theta=0.5, size=10000.0)
+    assert np.array_equal(a, c)
+
+
+def test_morton_and_sort_order_bit_exact(gpu):
+    from nbody_gb300 import scenes
+    b = scenes.plummer(20000, seed=31, rmax=15.0)
+    b[:50, :3] = 0.0                        # exactly on the centre planes
+    b[50:60, :3] = -np.float32(1e-30)       # tiny negatives: below every centre
+    b[60:70, :3] = b[70:80, :3]             # duplicated codes (ties by index)
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        for tree_box in (0, 1):
+            p = gpu.params(mode=gpu.MODE_NLOGN, size=64.0, tree_box=tree_box)
+            codes, order, box = ctx.morton(p)
+            if tree_box == 0:
+                assert list(box) == [-32.0, -32.0, -32.0, 64.0]
+            ref_codes = O.morton63(b[:, :3], box[:3], 2.0 ** 21 / box[3])
+            ref_order = O.sort_order(ref_codes)
+            assert np.array_equal(order, ref_order)
+            assert np.array_equal(codes, ref_codes[ref_order])
+
+
+def test_morton_cells_are_reference_cells(gpu):
+    """Every body's level-L Morton digit is its reference octant (bits flipped) in the
+    reference's own tree (golden node array of the 4096-body cube)."""
+    g = golden("cube_4096.npz")
+    b = g["bodies"]
+    nodes = np.frombuffer(g["nodes"].tobytes(), dtype=O.NODE_DTYPE)
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        codes, order, box = ctx.morton(gpu.params(mode=gpu.MODE_NLOGN, size=10000.0))
+    inv = np.empty_like(order)
+    inv[order] = np.arange(len(order))
+    for i in range(0, len(b), 37):
+        code = int(codes[inv[i]])
+        idx, level = 0, 0
+        while nodes[idx]["children"] != 0:
+            c = nodes[idx]["center"]
+            q = int(b[i, 0] < c[0]) | (int(b[i, 1] < c[1]) << 1) | (int(b[i, 2] < c[2]) << 2)
+            assert ((code >> (3 * (20 - level))) & 7) == q ^ 7
+            idx = nodes[idx]["children"] + q
+            level += 1
+
+
+@pytest.mark.parametrize("n", [100, 2000])
+def test_bh_theta_convention(gpu, n):
+    """test_bhtree.cpp:259-367 on the GPU: larger theta is more accurate and does more work.
+    The reference pins the loose error below 3.0 at its N = 100; at N = 2000 the GPU's
+    errors are pinned to the oracle octree's errors for the same inputs instead."""
+    g = np.random.default_rng(11)
+    p = np.clip(g.normal(0, 0.5, (n, 3)), -1, 1).astype(np.float32) * 100
+    b = np.zeros((n, 12), np.float32)
+    b[:, :3] = p
+    b[:, 7] = 1
+    exact = O.direct_f64(b[:, [0, 1, 2, 7]], 1.0, 0.0, O.LAW_CUTOFF)
+    mean_force = np.linalg.norm(exact, axis=1).mean()
+    loose, sl = bh_accel(gpu, b, theta=0.5, size=200.0)
+    tight, st = bh_accel(gpu, b, theta=8.0, size=200.0)
+    el = np.linalg.norm(loose - exact, axis=1).max() / mean_force
+    et = np.linalg.norm(tight - exact, axis=1).max() / mean_force
+    assert et < el and et < 0.05
+    assert st["interactions"] > sl["interactions"] > 0
+    assert st["interactions"] < n * n
+    t = O.Tree(200.0)
+    t.build(b, 200.0)
+    ol, _ = t.accel(b, 0.5, 1.0)
+    ot, _ = t.accel(b, 8.0, 1.0)
+    assert el <= 1.01 * np.linalg.norm(ol - exact, axis=1).max() / mean_force + 1e-6
+    assert et <= 1.01 * np.linalg.norm(ot - exact, axis=1).max() / mean_force + 1e-6
+    if n == 100:
+        assert el < 3.0
+
+
+@pytest.mark.parametrize("n", [2, 3, 5, 33, 257])
+def test_bh_small_sizes(gpu, n):
+    from nbody_gb300 import scenes
+    b = scenes.plummer(n, seed=5 + n, rmax=10.0)
+    acc, _ = bh_accel(gpu, b, theta=0.5, size=64.0)
+    ref, _ = O.barnes_hut(b, 64.0, 0.5, 1.0)
+    err = np.linalg.norm(acc - ref[:, 8:11], axis=1) / term_scale(b)
+    assert np.all(np.isfinite(acc)) and err.max() <= TOL
+
+
+def test_bh_one_body_and_empty(gpu):
+    b = np.zeros((1, 12), np.float32)
+    b[0, 7] = 5.0
+    acc, _ = bh_accel(gpu, b, theta=0.5, size=64.0)
+    assert np.all(acc == 0)
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(np.zeros((0, 12), np.float32))
+        ctx.update(gpu.params(mode=gpu.MODE_NLOGN, dt=0.1), steps=2)
+        ctx.synchronize()
+
+
+def test_bh_coincident_and_outside_bodies(gpu):
+    """Coincident bodies (a bucket of identical codes) and bodies outside the root box
+    (placed in edge cells, as the reference's quadrant test does)."""
+    from nbody_gb300 import scenes
+    b = scenes.plummer(3000, seed=8, rmax=10.0)
+    b[100:110, :3] = b[99, :3]              # 11 coincident bodies
+    b[200:205, 0] = 80.0                    # outside a 64 box
+    b[205:210, 1] = -90.0
+    acc, _ = bh_accel(gpu, b, theta=0.5, size=64.0)
+    ref, _ = O.barnes_hut(b, 64.0, 0.5, 1.0)
+    assert np.all(np.isfinite(acc))
+    err = np.linalg.norm(acc - ref[:, 8:11], axis=1) / term_scale(b)
+    # coincident bodies sit below the reference's FLT_EPSILON merge size and are merged
+    # there (bhtree.cpp:36-42); here they are one bucket applied body by body. The median
+    # body sits ~3e-6 from the reference: its FP32 running-mean centres of mass
+    # (bhtree.cpp:87-95) against the FP64 sums here.
+    assert np.median(err) <= 1e-5 and (err > TOL).sum() <= 15
+
+
+def test_bh_two_plummer_sampled(gpu):
+    """Config 2 inputs (two Plummer spheres, 2 x 131072), auto root box, softened law,
+    against the oracle's restated octree on sampled targets (same root box)."""
+    from nbody_gb300 import scenes
+    b = scenes.two_plummer(131072)
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        p = gpu.params(mode=gpu.MODE_NLOGN, theta=0.5, law=gpu.LAW_CUTOFF, size=64.0)
+        _, _, box = ctx.morton(p)
+        ctx.accelerate(p)
+        acc = ctx.download_bodies()[:, 8:11]
+    assert list(box) == [-32.0, -32.0, -32.0, 64.0]
+    assert np.all(np.isfinite(acc))
+    tg = np.random.default_rng(4).choice(len(b), 2048, replace=False)
+    t = O.Tree(64.0)
+    t.build(b, 64.0)
+    ref, _ = t.accel(b, 0.5, 1.0, targets=tg)
+    err = np.linalg.norm(acc[tg] - ref, axis=1) / term_scale(b, tg)
+    assert np.median(err) <= 1e-5 and (err > TOL).sum() <= 10, err.max()
+
+
+def test_bh_update_steps(gpu):
+    """BH update vs the reference's CPU Barnes-Hut stepping (5 steps, wrap on)."""
+    g = golden("disk_512.npz")
+    b = g["bodies"]
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        ctx.update(gpu.params(mode=gpu.MODE_NLOGN, theta=0.5, dt=1 / 120, size=10000.0, wrap=True), steps=5)
+        out = ctx.download_bodies()
+    ref = b.copy()
+    for _ in range(5):
+        ref, _ = O.barnes_hut(ref, 10000.0, 0.5, 1.0)
+        ref = O.integrate(ref, 1 / 120, 10000.0, True)
+    assert np.abs(out[:, :3] - ref[:, :3]).max() < 1e-3
