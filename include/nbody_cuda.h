@@ -216,6 +216,19 @@ int nbody_cuda_bh_stats(nbody_cuda* ctx, uint64_t out[3]);
 int nbody_cuda_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* codes,
                       uint32_t* order, double box[4]);
 
+/* --- precision forms --------------------------------------------------------------------- */
+
+/* Direct-sum accelerations of the listed bodies only (targets[k] in [0, count)), against all
+ * bodies, with p->precision COMPENSATED or FP64; results in FP64, 3 per target, before the
+ * rounding to float that nbody_cuda_accelerate applies. Synchronous. For error statistics
+ * on sampled targets at full size. No reference counterpart (the reference is FP32 only). */
+int nbody_cuda_accel_sampled(nbody_cuda* ctx, const nbody_step_params* p, const int64_t* targets,
+                             size_t nt, double* acc_out);
+
+/* The FP64 origin of the split-precision state (xyz) and the power-of-two edge it was
+ * aligned to; valid after a COMPENSATED or FP64 step. Synchronous. */
+int nbody_cuda_split_origin(nbody_cuda* ctx, double out[4]);
+
 /* --- introspection ------------------------------------------------------------------- */
 
 /* Kernel launches this context queued since creation (all entry points). */
@@ -229,6 +242,10 @@ int nbody_cuda_last_direct_config(const nbody_cuda* ctx, int* targets_per_thread
  * FFMA), scalar FFMA and packed FFMA2 chains; the denominator of the direct-sum
  * roofline. Synchronous; takes well under a second. */
 int nbody_cuda_calibrate_fp32(nbody_cuda* ctx, double* tflops_scalar, double* tflops_packed);
+
+/* Measured FP64 DFMA throughput in TFLOP/s (2 flop per DFMA); the denominator of the FP64
+ * form's roofline. Synchronous. */
+int nbody_cuda_calibrate_fp64(nbody_cuda* ctx, double* tflops);
 
 #ifdef __cplusplus
 }

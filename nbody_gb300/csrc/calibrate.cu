@@ -87,3 +87,60 @@ extern "C" int nbody_cuda_calibrate_fp32(nbody_cuda* ctx, double* tflops_scalar,
         *tflops_packed = res[1];
     return NBODY_OK;
 }
+
+namespace nbg
+{
+    __global__ void __launch_bounds__(256) dfma_peak_kernel(double* out, const int iters, const double a, const double b)
+    {
+        double v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            v[k] = threadIdx.x * 1e-3 + k;
+        for (int i = 0; i < iters; ++i)
+        {
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                v[k] = fma(v[k], a, b);
+        }
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            s += v[k];
+        out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+    }
+}
+
+extern "C" int nbody_cuda_calibrate_fp64(nbody_cuda* ctx, double* tflops)
+{
+    using namespace nbg;
+    if (!ctx || !tflops)
+        return NBODY_ERR_INVALID;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int blocks = sms * 4, threads = 256, iters = 1 << 10;
+    if (const int st = ensure_scratch(ctx, static_cast<size_t>(blocks) * threads * sizeof(double)))
+        return st;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep)
+    {
+        cudaEventRecord(e0, ctx->stream);
+        dfma_peak_kernel<<<blocks, threads, 0, ctx->stream>>>(static_cast<double*>(ctx->scratch), iters, 0.999, 1e-3);
+        ++ctx->launches;
+        cudaEventRecord(e1, ctx->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best)
+            best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return ctx_cuda_fail(ctx, e, "calibration kernel");
+    *tflops = static_cast<double>(blocks) * threads * iters * 8.0 * 2.0 / (best * 1e-3) / 1e12;
+    return NBODY_OK;
+}

@@ -226,6 +226,7 @@ void nbody_cuda_destroy(nbody_cuda* ctx)
     if (ctx->stream)
         cudaStreamSynchronize(ctx->stream);
     release_bh(ctx);
+    release_precise(ctx);
     cudaFree(ctx->pm);
     cudaFree(ctx->vr);
     cudaFree(ctx->acc);
@@ -583,8 +584,8 @@ namespace
     {
         if (p->precision == NBODY_PREC_COMPENSATED)
             return precise_integrate(ctx, p);
-        if (const int st = sync_precise_positions(ctx))
-            return st;
+        // an FP32 step moves the float positions past the split state: rebuild it later
+        ctx->origin_valid = false;
         return do_integrate(ctx, p);
     }
 }
@@ -652,6 +653,25 @@ int nbody_cuda_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* cod
     if (const int st = check_params(ctx, p))
         return st;
     return bh_morton(ctx, p, codes, order, box);
+}
+
+int nbody_cuda_accel_sampled(nbody_cuda* ctx, const nbody_step_params* p, const int64_t* targets, size_t nt,
+                             double* acc_out)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    if (nt && (!targets || !acc_out))
+        return fail(ctx, NBODY_ERR_INVALID, "null target list or output");
+    return precise_sampled(ctx, p, targets, nt, acc_out);
+}
+
+int nbody_cuda_split_origin(nbody_cuda* ctx, double out[4])
+{
+    if (!ctx || !out)
+        return NBODY_ERR_INVALID;
+    return precise_origin(ctx, out);
 }
 
 // --- caller-owned device buffers -----------------------------------------------------------

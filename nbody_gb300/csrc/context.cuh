@@ -74,6 +74,9 @@ namespace nbg
     int precise_integrate(nbody_cuda* ctx, const nbody_step_params* p);
     int sync_precise_positions(nbody_cuda* ctx);
     void release_precise(nbody_cuda* ctx);
+    int precise_sampled(nbody_cuda* ctx, const nbody_step_params* p, const int64_t* targets, size_t nt,
+                        double* out);
+    int precise_origin(nbody_cuda* ctx, double out[4]);
 
     // bh.cu
     int bh_accelerate(nbody_cuda* ctx, const nbody_step_params* p);

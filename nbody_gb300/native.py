@@ -31,6 +31,7 @@ EXPORTS = (
     "nbody_cuda_dev_accel_soa", "nbody_cuda_dev_accel_aos", "nbody_cuda_dev_integrate_soa",
     "nbody_cuda_launch_count", "nbody_cuda_last_direct_config", "nbody_cuda_calibrate_fp32",
     "nbody_cuda_dev_accel_soa_noalloc", "nbody_cuda_bh_stats", "nbody_cuda_morton",
+    "nbody_cuda_accel_sampled", "nbody_cuda_split_origin", "nbody_cuda_calibrate_fp64",
 )
 
 
@@ -92,6 +93,9 @@ def lib() -> C.CDLL:
         "nbody_cuda_dev_accel_soa_noalloc": ([vp, vp, vp, sz, P, vp], C.c_int),
         "nbody_cuda_bh_stats": ([vp, C.POINTER(C.c_uint64)], C.c_int),
         "nbody_cuda_morton": ([vp, P, vp, vp, C.POINTER(C.c_double)], C.c_int),
+        "nbody_cuda_accel_sampled": ([vp, P, vp, sz, vp], C.c_int),
+        "nbody_cuda_split_origin": ([vp, C.POINTER(C.c_double)], C.c_int),
+        "nbody_cuda_calibrate_fp64": ([vp, C.POINTER(C.c_double)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -221,6 +225,22 @@ class Context:
         box = (C.c_double * 4)()
         self.check(lib().nbody_cuda_morton(self.h, C.byref(p), _ptr(codes), _ptr(order), box))
         return codes, order, np.array(box[:])
+
+    def accel_sampled(self, p: StepParams, targets) -> np.ndarray:
+        t = np.ascontiguousarray(targets, np.int64)
+        out = np.zeros((len(t), 3), np.float64)
+        self.check(lib().nbody_cuda_accel_sampled(self.h, C.byref(p), _ptr(t), len(t), _ptr(out)))
+        return out
+
+    def split_origin(self) -> np.ndarray:
+        out = (C.c_double * 4)()
+        self.check(lib().nbody_cuda_split_origin(self.h, out))
+        return np.array(out[:])
+
+    def calibrate_fp64(self) -> float:
+        v = C.c_double()
+        self.check(lib().nbody_cuda_calibrate_fp64(self.h, C.byref(v)))
+        return v.value
 
     def calibrate_fp32(self) -> tuple[float, float]:
         s, p = C.c_double(), C.c_double()

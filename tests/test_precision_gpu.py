@@ -1,0 +1,180 @@
+"""Split-precision (compensated) and FP64 forms on the GPU, against the FP64 oracle.
+
+Bars (BASELINE: compensated median relative acceleration error <= 1e-6 against FP64):
+  * compensated direct sum: median |a - a64| / |a64| <= 1e-6; per body
+    |a - a64| <= 2e-6 * sum_j |a_ij| (the float rounding of the result alone is ~6e-8 |a|);
+  * FP64 direct sum: |a - a64| <= 1e-12 * sum_j |a_ij| (different summation order only);
+  * compensated integration tracks an FP64 integration of the same steps closer than the
+    plain FP32 integrator does.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def f64_ref(b, eps2, law, targets=None):
+    # eps2 reaches the kernels as a float (nbody_step_params), so the oracle gets that value
+    return O.direct_f64(b[:, [0, 1, 2, 7]], 1.0, float(np.float32(eps2)), law, radius=b[:, 3], targets=targets,
+                        with_scale=True)
+
+
+def rel_errors(acc, ref, scale):
+    d = np.linalg.norm(np.asarray(acc, np.float64) - ref, axis=1)
+    mag = np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
+    return d / mag, d / np.maximum(scale, 1e-300)
+
+
+@pytest.mark.parametrize("layout", [0, 1], ids=["soa", "aos"])
+def test_compensated_plummer_4096(gpu, layout):
+    from nbody_gb300 import scenes
+    b = scenes.plummer(4096, seed=1001)
+    p = gpu.params(law=gpu.LAW_SOFTENED, eps2=1e-4, precision=gpu.PREC_COMPENSATED)
+    with gpu.Context(layout) as ctx:
+        ctx.upload_bodies(b)
+        ctx.accelerate(p)
+        acc = ctx.download_bodies()[:, 8:11]
+        sampled = ctx.accel_sampled(p, np.arange(0, 4096, 7))
+    ref, scale = f64_ref(b, 1e-4, O.LAW_SOFTENED)
+    rel, sc = rel_errors(acc, ref, scale)
+    assert np.median(rel) <= 1e-6 and sc.max() <= 2e-6, (np.median(rel), sc.max())
+    # the sampled FP64 results round to exactly the stored float accelerations
+    assert np.array_equal(sampled.astype(np.float32), acc[::7])
+    rel_s, _ = rel_errors(sampled, ref[::7], scale[::7])
+    assert np.median(rel_s) <= 1e-6
+
+
+def test_compensated_reference_law(gpu):
+    g = golden("cube_4096.npz")
+    b = g["bodies"]
+    p = gpu.params(law=gpu.LAW_CUTOFF, precision=gpu.PREC_COMPENSATED)
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        ctx.accelerate(p)
+        acc = ctx.download_bodies()[:, 8:11]
+    ref, scale = f64_ref(b, 0.0, O.LAW_CUTOFF)
+    rel, sc = rel_errors(acc, ref, scale)
+    assert np.median(rel) <= 1e-6 and sc.max() <= 2e-6
+
+
+def test_fp64_matches_oracle(gpu):
+    from nbody_gb300 import scenes
+    b = scenes.uniform_cube(20000, seed=9)
+    tg = np.arange(0, 20000, 13)
+    for law, eps2 in ((gpu.LAW_SOFTENED, 1e-6), (gpu.LAW_CUTOFF, 0.0)):
+        with gpu.Context() as ctx:
+            ctx.upload_bodies(b)
+            got = ctx.accel_sampled(gpu.params(law=law, eps2=eps2, precision=gpu.PREC_FP64), tg)
+            ctx.accelerate(gpu.params(law=law, eps2=eps2, precision=gpu.PREC_FP64))
+            full = ctx.download_bodies()[:, 8:11]
+        ref, scale = f64_ref(b, eps2, law, targets=tg)
+        _, sc = rel_errors(got, ref, scale)
+        assert sc.max() <= 1e-12, sc.max()
+        assert np.array_equal(full[tg], got.astype(np.float32))
+
+
+def test_config3_forms_sampled(gpu):
+    """Config 3 (N = 2^20 uniform cube, log-normal masses, eps = 1e-3): error per form on
+    sampled targets against the FP64 oracle."""
+    from nbody_gb300 import scenes
+    n = 1 << 20
+    b = scenes.uniform_cube(n, seed=1003)
+    tg = np.random.default_rng(3).choice(n, 256, replace=False)
+    ref, scale = f64_ref(b, 1e-6, O.LAW_SOFTENED, targets=tg)
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        plain = gpu.params(law=gpu.LAW_SOFTENED, eps2=1e-6)
+        comp = gpu.params(law=gpu.LAW_SOFTENED, eps2=1e-6, precision=gpu.PREC_COMPENSATED)
+        ctx.accelerate(plain)
+        a32 = ctx.download_bodies()[tg, 8:11]
+        a_c = ctx.accel_sampled(comp, tg)
+        a64 = ctx.accel_sampled(gpu.params(law=gpu.LAW_SOFTENED, eps2=1e-6, precision=gpu.PREC_FP64), tg)
+    r32, _ = rel_errors(a32, ref, scale)
+    rc, _ = rel_errors(a_c, ref, scale)
+    r64, _ = rel_errors(a64, ref, scale)
+    assert np.median(rc) <= 1e-6, np.median(rc)
+    assert np.median(rc) < np.median(r32)
+    assert np.median(r64) <= 1e-12
+
+
+def test_split_origin_is_aligned(gpu):
+    from nbody_gb300 import scenes
+    b = scenes.plummer(1000, seed=2)
+    b[:, 0] += 1000.0          # far from the origin: the split state keeps offsets small
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        ctx.accelerate(gpu.params(law=gpu.LAW_SOFTENED, eps2=1e-4, precision=gpu.PREC_COMPENSATED))
+        o = ctx.split_origin()
+    e = o[3]
+    assert e > 0 and np.log2(e) == np.round(np.log2(e))
+    assert np.all(np.mod(o[:3], e) == 0)
+    # x straddles 1000 far from 0: origin within e/2 of the centre; y, z straddle 0: origin 0
+    assert o[0] != 0 and np.all(np.abs(b[:, 0] - o[0]) <= e)
+    assert o[1] == 0 and o[2] == 0
+
+
+def integrate_f64(pos, vel, mass, eps2, dt, steps):
+    for _ in range(steps):
+        a = O.direct_f64_pos(pos, mass, 1.0, eps2)
+        vel = vel + a * dt
+        pos = pos + vel * dt
+    return pos, vel
+
+
+def test_compensated_integration_tracks_fp64(gpu):
+    """Far from the origin (x ~ 1000), plain FP32 positions lose ~6e-5 per update; the
+    FP64-origin + FP32-offset state with Kahan updates follows the FP64 run closely."""
+    from nbody_gb300 import scenes
+    b = scenes.plummer(512, seed=21)
+    b[:, 0] += 1000.0
+    pos0 = b[:, :3].astype(np.float64)
+    vel0 = b[:, 4:7].astype(np.float64)
+    m = b[:, 7].astype(np.float64)
+    steps, dt, eps2 = 200, 1e-3, 1e-4
+    ref_pos, ref_vel = integrate_f64(pos0, vel0, m, eps2, dt, steps)
+    errs = {}
+    for prec in (gpu.PREC_FP32, gpu.PREC_COMPENSATED):
+        with gpu.Context() as ctx:
+            ctx.upload_bodies(b)
+            ctx.update(gpu.params(law=gpu.LAW_SOFTENED, eps2=eps2, dt=dt, precision=prec, size=0.0), steps=steps)
+            out = ctx.download_bodies()
+        errs[prec] = np.abs(out[:, :3] - ref_pos).max()
+    assert errs[gpu.PREC_COMPENSATED] < 0.1 * errs[gpu.PREC_FP32], errs
+    assert errs[gpu.PREC_COMPENSATED] < 2e-4, errs      # float rounding of x ~ 1000 is 6e-5
+
+
+def test_precision_errors_reported(gpu):
+    b = golden("disk_512.npz")["bodies"]
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        with pytest.raises(gpu.NbodyError) as e:
+            ctx.update(gpu.params(precision=gpu.PREC_COMPENSATED, wrap=True, size=1000.0, dt=0.01))
+        assert e.value.status == gpu.ERR_UNSUPPORTED
+        with pytest.raises(gpu.NbodyError) as e:
+            ctx.accelerate(gpu.params(precision=gpu.PREC_FP64, mode=gpu.MODE_NLOGN))
+        assert e.value.status == gpu.ERR_UNSUPPORTED
+        with pytest.raises(gpu.NbodyError) as e:
+            ctx.accel_sampled(gpu.params(precision=gpu.PREC_FP64), [0, 1, 512])
+        assert e.value.status == gpu.ERR_INVALID
+        ctx.accelerate(gpu.params(precision=gpu.PREC_COMPENSATED))     # still usable
+        ctx.synchronize()
+
+
+def test_bh_with_compensated_integration(gpu):
+    """Config 5's form: FP32 tree forces + compensated integration."""
+    from nbody_gb300 import scenes
+    b = scenes.two_plummer(4096)
+    p32 = gpu.params(mode=gpu.MODE_NLOGN, theta=0.75, law=gpu.LAW_SOFTENED, eps2=2.5e-5, dt=2.5e-4, size=0.0)
+    pc = gpu.params(mode=gpu.MODE_NLOGN, theta=0.75, law=gpu.LAW_SOFTENED, eps2=2.5e-5, dt=2.5e-4, size=0.0,
+                    precision=gpu.PREC_COMPENSATED)
+    outs = []
+    for p in (p32, pc):
+        with gpu.Context() as ctx:
+            ctx.upload_bodies(b)
+            ctx.update(p, steps=10)
+            outs.append(ctx.download_bodies())
+    assert np.all(np.isfinite(outs[1]))
+    assert np.abs(outs[0][:, :3] - outs[1][:, :3]).max() < 1e-4
