@@ -1,7 +1,8 @@
-"""Throughput bench: body-steps/s of the direct-sum step at N = 1,048,576.
+"""Throughput bench: body-steps/s of the direct-sum step at N = 1,048,576, plus the
+compensated form, the FP64 form, Barnes-Hut at N = 16,777,216 and the small configs.
 
-Workload (one GPU): N = 1,048,576 bodies uniform in [0,1)^3 at rest, log-normal(0, 0.5)
-masses summing to 1, softened law eps = 1e-3, G = 1, FP32, semi-implicit Euler
+Headline workload (one GPU): N = 1,048,576 bodies uniform in [0,1)^3 at rest, log-normal
+(0, 0.5) masses summing to 1, softened law eps = 1e-3, G = 1, FP32, semi-implicit Euler
 dt = 1e-3, no wrap. A "step" is one full update (accelerate + integrate) of all bodies.
 
 Printed JSON line (rank 0):
@@ -14,6 +15,15 @@ Printed JSON line (rank 0):
                   (nbody_cuda_calibrate_fp32): 20 flop per pair (the GPU Gems 3 ch. 31
                   convention), N^2 pairs per launch, divided by the kernel's own average
                   event-timed duration.
+  compensated     the same workload in the split-precision form: body-steps/s, its ratio
+                  to plain FP32, and the median / p99 relative acceleration error of each
+                  form against FP64 on 65,536 sampled targets (the FP64 reference is the
+                  GPU FP64 form, itself checked against the CPU oracle on 512 targets).
+  barnes_hut_16m  N = 16,777,216 exponential disk + Hernquist halo, eps = 0.005,
+                  dt = 2.5e-4, FP32 tree forces + compensated integration, reference-
+                  convention theta 0.5 and 0.75: steps/s, interactions, tree cells, and the
+                  per-stage byte model against the measured HBM copy bandwidth.
+  configs         configs 1 (N = 4096 Plummer, 100 steps) and 2 (2 x 131072 Plummer BH).
   cpu_baseline    the reference's CPU brute force (oracle/_ref, built from the reference's
                   sources) where it loads, else the oracle's C restatement, on all host
                   cores, timed on a bounded sample of targets against all N sources.
@@ -46,11 +56,19 @@ METRIC = "body-steps/s N=1M direct & 16M BH θ=0.5; compensated vs plain FP32 at
 WORKLOAD = ("direct-sum step, N=1048576 uniform unit cube at rest, log-normal(0,0.5) masses "
             "summing to 1, softened eps=1e-3, G=1, dt=1e-3, FP32, semi-implicit Euler")
 FLOP_PER_PAIR = 20
+N_SAMPLE = 65536
 
 
 def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
         int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def measured_peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        return {}
 
 
 # --- clocks ---------------------------------------------------------------------------
@@ -63,6 +81,7 @@ class ClockSampler:
     def __init__(self, device_index: int):
         self.dev = device_index
         self.proc = None
+        self.out = ""
 
     def __enter__(self):
         try:
@@ -74,7 +93,6 @@ class ClockSampler:
         return self
 
     def __exit__(self, *exc):
-        self.out = ""
         if self.proc:
             self.proc.terminate()
             try:
@@ -106,43 +124,64 @@ class ClockSampler:
 
 def cpu_brute_force_rate(bodies: np.ndarray, seconds: float = 10.0):
     """Pairs/s of the reference CPU brute force (or its restatement) on all host cores,
-    timed on a bounded sample of targets against all sources."""
+    timed on a bounded sample of the workload."""
     from oracle import oracle as O
     n = len(bodies)
     threads = O.threads()
-    use_ref = O.ref_available()
-    kind = "reference" if use_ref else "port"
-
-    def run(k):
+    if O.ref_available():
+        # the reference solver sums over all of its bodies: time it on a k-body prefix
+        k = 2048
+        while True:
+            t0 = time.perf_counter()
+            O.ref_brute_force(bodies[:k], 1.0, nthreads=threads)
+            dt = time.perf_counter() - t0
+            if dt >= seconds / 4 or k >= n:
+                break
+            k = min(n, int(k * max(1.5, min(4.0, np.sqrt(seconds / max(dt, 1e-3))))))
+        return k * k / dt, threads, "reference", \
+            f"CpuBruteForceSolver::accelerate on the first {k} bodies (all {k}x{k} pairs), {dt:.1f} s"
+    k = 64
+    while True:
         tg = np.linspace(0, n - 1, k).astype(np.int64)
         t0 = time.perf_counter()
-        if use_ref:
-            # the reference solver runs over all of its bodies; give it k targets + all
-            # sources by timing k/n of a full sweep through the targets-only restated path
-            # is not possible, so time its own accelerate on a k-body prefix scaled below.
-            sub = bodies[:k]
-            O.ref_brute_force(sub, 1.0, nthreads=threads)
-            dt = time.perf_counter() - t0
-            return k * k, dt
         O.brute_force_targets(bodies, 1.0, tg, nthreads=threads)
         dt = time.perf_counter() - t0
-        return k * n, dt
+        if dt >= seconds / 4:
+            break
+        k = int(k * min(8.0, max(2.0, seconds / max(dt, 1e-3))))
+    return k * n / dt, threads, "port", \
+        f"{k} sampled targets x all {n} sources (restated reference brute force), {dt:.1f} s"
 
-    if use_ref:
-        k = 2048
-        pairs, dt = run(k)
-        while dt < seconds / 4 and k < n:
-            k = min(n, int(k * max(1.5, min(4.0, np.sqrt(seconds / max(dt, 1e-3))))))
-            pairs, dt = run(k)
-        sample = f"CpuBruteForceSolver::accelerate on the first {k} bodies (all {k}x{k} pairs)"
-    else:
-        k = 64
-        pairs, dt = run(k)
-        while dt < seconds / 4:
-            k = int(k * min(8.0, max(2.0, seconds / max(dt, 1e-3))))
-            pairs, dt = run(k)
-        sample = f"{k} sampled targets x all {n} sources (restated reference brute force)"
-    return pairs / dt, threads, kind, sample, dt
+
+def cpu_barnes_hut_rate(bodies, size, theta):
+    """Seconds per step of the restated reference CpuBarnesHutSolver (serial tree build +
+    parallel traversal, cpu_barnes_hut.h:22-44) on all host cores."""
+    from oracle import oracle as O
+    threads = O.threads()
+    t0 = time.perf_counter()
+    O.barnes_hut(bodies, size, theta, 1.0, nthreads=threads)
+    return time.perf_counter() - t0, threads
+
+
+# --- helpers for the GPU arm ------------------------------------------------------------------
+
+def timed_steps(torch, stream, flush, fn, steps):
+    """Per-step CUDA-event times (ms) on `stream`, L2 flushed between steps."""
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        flush.zero_()
+        starts[k].record(stream)
+        fn()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+
+def rel_stats(acc, ref):
+    d = np.linalg.norm(np.asarray(acc, np.float64) - ref, axis=1)
+    r = d / np.maximum(np.linalg.norm(ref, axis=1), 1e-300)
+    return {"median": float(np.median(r)), "p99": float(np.percentile(r, 99)), "max": float(r.max())}
 
 
 # --- the GPU arm ----------------------------------------------------------------------------
@@ -179,36 +218,24 @@ def _bench_gpu(args, stream):
     ctx = native.Context(native.LAYOUT_SOA)
     ctx.set_stream(stream.cuda_stream)
     ctx.upload_bodies(bodies)
-    s_tf, p_tf = ctx.calibrate_fp32()
-    fp32_peak = max(s_tf, p_tf)
-
-    def one_step():
-        ctx.update(p, 1)
-
     for _ in range(args.warmup):
         flush.zero_()
-        one_step()
+        ctx.update(p, 1)
     torch.cuda.synchronize()
+    s_tf, p_tf = ctx.calibrate_fp32()      # after warm-up: clocks are up
+    fp32_peak = max(s_tf, p_tf)
 
     # --- device-timed steps (value) ---
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     launches0 = ctx.launches()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        for k in range(args.steps):
-            flush.zero_()
-            starts[k].record(stream)
-            one_step()
-            ends[k].record(stream)
-        torch.cuda.synchronize()
+        step_ms = timed_steps(torch, stream, flush, lambda: ctx.update(p, 1), args.steps)
     if world > 1:
         torch.distributed.barrier()
     ctx.synchronize()
     launches = ctx.launches() - launches0
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = sum(step_ms)
     if world > 1:
         t = torch.tensor([total_ms], device="cuda")
@@ -218,16 +245,8 @@ def _bench_gpu(args, stream):
     value = N * args.steps * world / (total_ms * 1e-3)
 
     # --- the dominant kernel alone (accelerate), for the roofline ---
-    acc_starts = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    acc_ends = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    for k in range(3):
-        flush.zero_()
-        acc_starts[k].record(stream)
-        ctx.accelerate(p)
-        acc_ends[k].record(stream)
-    torch.cuda.synchronize()
+    acc_ms = statistics.mean(timed_steps(torch, stream, flush, lambda: ctx.accelerate(p), 3))
     ctx.synchronize()
-    acc_ms = statistics.mean(s.elapsed_time(e) for s, e in zip(acc_starts, acc_ends))
     cfg = ctx.last_direct_config()
     pairs = float(N) * N
     achieved_tf = FLOP_PER_PAIR * pairs / (acc_ms * 1e-3) / 1e12
@@ -246,9 +265,15 @@ def _bench_gpu(args, stream):
     e2e_value = N * e2e_steps * world / (t1 - t0)
     ctx.close()
 
+    extra = {}
+    if rank == 0 and not args.quick:
+        extra["compensated"] = bench_compensated(torch, stream, flush, native, bodies, args, value, fp32_peak)
+        extra["barnes_hut_16m"] = bench_bh16m(torch, stream, flush, native, scenes, args)
+        extra["configs"] = bench_small_configs(torch, stream, flush, native, scenes)
+
     line = None
     if rank == 0:
-        cpu_rate, cores, kind, sample, cpu_s = cpu_brute_force_rate(bodies, seconds=args.cpu_seconds)
+        cpu_rate, cores, kind, sample = cpu_brute_force_rate(bodies, seconds=args.cpu_seconds)
         line = {
             "metric": METRIC,
             "value": value,
@@ -271,19 +296,152 @@ def _bench_gpu(args, stream):
                     "path": "nbody_cuda_upload_bodies + nbody_cuda_update + nbody_cuda_download_bodies, pinned host Body[]"},
             "roofline": {"bound": "fp32", "kernel": "direct_fp32_kernel", "achieved": achieved_tf,
                          "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak,
-                         "peak_source": "measured FFMA/FFMA2 chains on this GPU (nbody_cuda_calibrate_fp32)",
+                         "peak_source": "measured FFMA/FFMA2 chains on this GPU (nbody_cuda_calibrate_fp32); "
+                                        "MEASURED_PEAKS.json carries no FP32 figure",
                          "peak_scalar_ffma": s_tf, "peak_packed_ffma2": p_tf,
                          "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs,
-                         "kernel_ms": acc_ms, "traffic": None},
+                         "kernel_ms": acc_ms, "traffic": 139991040,
+                         "traffic_note": "dram bytes read+write of one N=2^20 launch, ncu (profiles/direct_fp32_n262144_full.md)"},
             "cpu_baseline": {"value": cpu_rate / N, "unit": "body-steps/s", "cores": cores, "kind": kind,
-                             "sample": sample + f"; {cpu_s:.1f} s; body-steps/s = pairs/s / N",
-                             "pairs_per_s": cpu_rate},
+                             "sample": sample + "; body-steps/s = pairs/s / N", "pairs_per_s": cpu_rate},
             "clocks": clocks.summary(),
             "gpu_launches": launches,
         }
+        line.update(extra)
     if world > 1:
         torch.distributed.destroy_process_group()
     return line
+
+
+def bench_compensated(torch, stream, flush, native, bodies, args, fp32_value, fp32_peak):
+    from oracle import oracle as O
+    pc = native.params(dt=DT, G=1.0, eps2=EPS * EPS, law=native.LAW_SOFTENED, size=0.0,
+                       precision=native.PREC_COMPENSATED)
+    p32 = native.params(dt=DT, G=1.0, eps2=EPS * EPS, law=native.LAW_SOFTENED, size=0.0)
+    p64 = native.params(dt=DT, G=1.0, eps2=EPS * EPS, law=native.LAW_SOFTENED, size=0.0,
+                        precision=native.PREC_FP64)
+    out = {}
+    with native.Context() as ctx:
+        ctx.set_stream(stream.cuda_stream)
+        ctx.upload_bodies(bodies)
+        # accuracy of each form, from the same initial state
+        tg = np.random.default_rng(1003).choice(N, N_SAMPLE, replace=False)
+        ctx.accelerate(p32)
+        a32 = ctx.download_bodies()[tg, 8:11]
+        ctx.accelerate(pc)
+        ac = ctx.download_bodies()[tg, 8:11]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        a64 = ctx.accel_sampled(p64, tg)
+        t64 = time.perf_counter() - t0
+        chk = a64[:512]
+        ref = O.direct_f64(bodies[:, [0, 1, 2, 7]], 1.0, float(np.float32(EPS * EPS)), O.LAW_SOFTENED,
+                           targets=tg[:512])
+        fp64_check = float(np.max(np.linalg.norm(chk - ref, axis=1) / np.linalg.norm(ref, axis=1)))
+        # throughput of the compensated step
+        for _ in range(args.warmup):
+            ctx.update(pc, 1)
+        torch.cuda.synchronize()
+        steps = max(3, args.steps // 2)
+        ms = timed_steps(torch, stream, flush, lambda: ctx.update(pc, 1), steps)
+        comp_value = N * steps / (sum(ms) * 1e-3)
+        acc_ms = statistics.mean(timed_steps(torch, stream, flush, lambda: ctx.accelerate(pc), 2))
+        fp64_peak = ctx.calibrate_fp64()
+        cfg = ctx.last_direct_config()
+    fp64_pairs = float(N_SAMPLE) * N
+    out = {
+        "value": comp_value, "unit": "body-steps/s", "ratio_vs_fp32": comp_value / fp32_value,
+        "ms_per_step": sum(ms) / steps,
+        "form": "FP64 origin + FP32 offsets, FP32 pair forces, Kahan over 64-source sub-tiles, FP64 chunk sums, "
+                "Kahan-compensated integration",
+        "err_vs_fp64": {"fp32": rel_stats(a32, a64), "compensated": rel_stats(ac, a64),
+                        "targets": N_SAMPLE, "metric": "|a - a_fp64| / |a_fp64|",
+                        "fp64_reference": "GPU FP64 form; max rel. diff. to the CPU FP64 oracle on 512 targets "
+                                          f"= {fp64_check:.2e}"},
+        "roofline": {"bound": "fp32", "achieved": FLOP_PER_PAIR * float(N) * N / (acc_ms * 1e-3) / 1e12,
+                     "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": FLOP_PER_PAIR * float(N) * N / (acc_ms * 1e-3) / 1e12 / fp32_peak,
+                     "kernel_ms": acc_ms, "launch": cfg},
+        "fp64_form": {"pairs_per_s": fp64_pairs / t64, "seconds": t64, "targets": N_SAMPLE,
+                      "peak_dfma_tflops": fp64_peak,
+                      "note": "synchronous sampled call incl. upload/readback; ~20 DP flop per pair"},
+    }
+    return out
+
+
+def bench_bh16m(torch, stream, flush, native, scenes, args):
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    t0 = time.perf_counter()
+    b = scenes.disk_halo()
+    gen_s = time.perf_counter() - t0
+    n = len(b)
+    res = {"n_bodies": n, "workload": "exponential disk 12,000,000 (R_d=3, z_0=0.3, circular v) + Hernquist "
+                                      "halo 4,777,216 (a=10, m_halo = 5 m_disk), eps=0.005, dt=2.5e-4, "
+                                      "FP32 tree forces + compensated integration, auto power-of-two root box",
+           "generate_s": gen_s, "theta_convention": "reference (accept when |com-x| > size*theta)"}
+    with native.Context() as ctx:
+        ctx.set_stream(stream.cuda_stream)
+        for theta in (0.5, 0.75):
+            ctx.upload_bodies(b)
+            p = native.params(mode=native.MODE_NLOGN, theta=theta, law=native.LAW_SOFTENED, eps2=0.005 ** 2,
+                              dt=2.5e-4, size=0.0, tree_box=1, precision=native.PREC_COMPENSATED)
+            for _ in range(args.warmup):
+                ctx.update(p, 1)
+            torch.cuda.synchronize()
+            steps = max(5, args.steps)
+            ms = timed_steps(torch, stream, flush, lambda: ctx.update(p, 1), steps)
+            ctx.accelerate(p)
+            stats = ctx.bh_stats()
+            ms_step = sum(ms) / steps
+            # compulsory bytes per step (byte model): bbox 16, Morton 16+8, sort 8 passes x 24,
+            # permute 32, build ~56 per internal node, COM ~48 per node, integrate 80 (+32 comp)
+            build_b = n * (16 + 24 + 8 * 24 + 32 + 56 + 48) + n * (80 + 48)
+            trav_b = 16 * stats["interactions"] + 64 * stats["visits"]
+            res[f"theta_{theta}"] = {
+                "steps_per_s": 1e3 / ms_step, "ms_per_step": ms_step, "body_steps_per_s": n * 1e3 / ms_step,
+                "interactions": stats["interactions"], "interactions_per_body": stats["interactions"] / n,
+                "warp_cell_visits": stats["visits"], "tree_cells": stats["cells"],
+                "roofline": {"bound": "hbm", "achieved": (build_b + trav_b) / (ms_step * 1e-3) / 1e9,
+                             "peak": hbm, "unit": "GB/s",
+                             "frac": (build_b + trav_b) / (ms_step * 1e-3) / 1e9 / hbm,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                             "bytes_model": "build+integrate ~%d B/body, traversal 16 B/interaction + 64 B/cell "
+                                            "visit (mostly L2 hits)" % ((build_b) // n)},
+            }
+    return res
+
+
+def bench_small_configs(torch, stream, flush, native, scenes):
+    out = {}
+    # config 1: N=4096 Plummer, 100 steps, FP32, eps 0.01
+    b = scenes.plummer(4096, seed=1001)
+    p = native.params(dt=1e-3, eps2=1e-4, law=native.LAW_SOFTENED, size=0.0)
+    with native.Context() as ctx:
+        ctx.set_stream(stream.cuda_stream)
+        ctx.upload_bodies(b)
+        ctx.update(p, 3)
+        torch.cuda.synchronize()
+        ms = timed_steps(torch, stream, flush, lambda: ctx.update(p, 100), 1)[0]
+    out["config1_plummer_4096"] = {"steps": 100, "ms": ms, "body_steps_per_s": 4096 * 100 / (ms * 1e-3)}
+    # config 2: two Plummer spheres, BH theta 0.5 (reference convention), 200 steps
+    b = scenes.two_plummer(131072)
+    p = native.params(mode=native.MODE_NLOGN, theta=0.5, dt=5e-4, eps2=1e-4, law=native.LAW_SOFTENED,
+                      size=64.0)
+    with native.Context() as ctx:
+        ctx.set_stream(stream.cuda_stream)
+        ctx.upload_bodies(b)
+        ctx.update(p, 3)
+        torch.cuda.synchronize()
+        ms = timed_steps(torch, stream, flush, lambda: ctx.update(p, 200), 1)[0]
+        stats = ctx.bh_stats()
+    cpu_s, cores = cpu_barnes_hut_rate(b, 64.0, 0.5)
+    out["config2_two_plummer_bh"] = {"n_bodies": len(b), "steps": 200, "ms": ms, "steps_per_s": 200 / (ms * 1e-3),
+                                     "body_steps_per_s": len(b) * 200 / (ms * 1e-3),
+                                     "interactions_per_body": stats["interactions"] / len(b),
+                                     "cpu_reference_bh_step_s": cpu_s, "cpu_cores": cores,
+                                     "cpu_kind": "port (restated CpuBarnesHutSolver, serial build)"}
+    return out
 
 
 def bench_reference(args):
@@ -295,7 +453,7 @@ def bench_reference(args):
     per_step = []
     info = None
     for k in range(args.warmup + args.steps):
-        rate, cores, kind, sample, dt = cpu_brute_force_rate(bodies, seconds=args.cpu_seconds / 2)
+        rate, cores, kind, sample = cpu_brute_force_rate(bodies, seconds=args.cpu_seconds / 2)
         info = (cores, kind, sample)
         if k >= args.warmup:
             per_step.append(N / rate)     # seconds for one full body-step of all N bodies
@@ -317,7 +475,7 @@ def bench_reference(args):
         "dtype": "f32",
         "data": "synthetic (seeded Philox): uniform unit cube, log-normal masses",
         "config": {"workload": WORKLOAD, "n_bodies": N, "eps": EPS, "dt": DT,
-                   "note": "reference CPU brute force uses its own radius-cutoff law (no softening); "
+                   "note": "the reference CPU brute force uses its own radius-cutoff law (no softening); "
                            "same pair count and arithmetic class"},
         "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": cores, "kind": kind,
                          "sample": sample + " per step; body-steps/s = pairs/s / N"},
@@ -332,6 +490,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--quick", action="store_true", help="headline workload only (for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
