@@ -216,6 +216,14 @@ int nbody_cuda_bh_stats(nbody_cuda* ctx, uint64_t out[3]);
 int nbody_cuda_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* codes,
                       uint32_t* order, double box[4]);
 
+/* The tree of the last Barnes-Hut accelerate in the reference's node layout: 48-byte
+ * bh::Node records (include/nbody/bhtree.h:13-22), root at index 0, 8 contiguous children
+ * per split node with child q in the reference's octant order (bounds.h:31-38), threaded
+ * `next` links, empty octants as massless leaves. Writes min(count, max_nodes) nodes (none
+ * when nodes is NULL) and the total into *count. This is what Solver::tree() returns for a
+ * tree-building variant (source/solvers/cpu_barnes_hut.h:46, sim.cpp:329-335). */
+int nbody_cuda_tree_export(nbody_cuda* ctx, void* nodes, size_t max_nodes, size_t* count);
+
 /* --- precision forms --------------------------------------------------------------------- */
 
 /* Direct-sum accelerations of the listed bodies only (targets[k] in [0, count)), against all

@@ -71,6 +71,9 @@ namespace nbg
         unsigned long long* stats = nullptr;   // [0] interactions, [1] node visits, [2] octree nodes
         const uint32_t* order = nullptr;       // sorted indices of the last build (keys/vals ping-pong)
         const uint64_t* codes = nullptr;
+        bool built = false;                    // a tree for built_n bodies is on the device
+        size_t built_n = 0;
+        uint64_t build_id = 0;
     };
 
     // ------------------------------------------------------------------------------------
@@ -647,7 +650,12 @@ namespace nbg
         if (e != cudaSuccess)
             return ctx_cuda_fail(ctx, e, "prefix sums");
         if (n < 2)
+        {
+            b.built = true;
+            b.built_n = n;
+            ++b.build_id;
             return NBODY_OK;
+        }
         const int m = ni - 1;
         karras_kernel<<<ceil_div(m, 256), 256, 0, s>>>(keys, ni, b.child, b.parent, b.range, b.prefix);
         ++L;
@@ -662,6 +670,9 @@ namespace nbg
         e = cudaGetLastError();
         if (e != cudaSuccess)
             return ctx_cuda_fail(ctx, e, "tree build");
+        b.built = true;
+        b.built_n = n;
+        ++b.build_id;
         return NBODY_OK;
     }
 
@@ -731,6 +742,49 @@ namespace nbg
                                               cudaMemcpyDeviceToHost, ctx->stream);
         if (e != cudaSuccess)
             return ctx_cuda_fail(ctx, e, "tree statistics readback");
+        return check_device_error(ctx);
+    }
+
+    uint64_t bh_build_id(const nbody_cuda* ctx)
+    {
+        return (ctx->bh && ctx->bh->built) ? ctx->bh->build_id : 0;
+    }
+
+    int bh_download(nbody_cuda* ctx, TreeSnapshot* out)
+    {
+        out->n = 0;
+        out->cells.clear();
+        out->codes.clear();
+        out->bodies.clear();
+        if (!ctx->bh || !ctx->bh->built)
+            return ctx_fail(ctx, NBODY_ERR_INVALID, "no Barnes-Hut tree has been built");
+        BhState& b = *ctx->bh;
+        const size_t n = b.built_n;
+        out->n = n;
+        out->build_id = b.build_id;
+        cudaStream_t s = ctx->stream;
+        out->codes.resize(n);
+        out->bodies.resize(n);
+        unsigned long long st[3] = { 0, 0, 0 };
+        cudaError_t e = cudaMemcpyAsync(out->codes.data(), b.codes, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(out->bodies.data(), b.spm, n * sizeof(float4), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&out->box, b.box, sizeof(BoxParams), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(st, b.stats, sizeof st, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess)
+            return ctx_cuda_fail(ctx, e, "tree readback");
+        const size_t cells = n >= 2 ? static_cast<size_t>(st[2]) : 0;
+        out->cells.resize(cells);
+        if (cells)
+        {
+            e = cudaMemcpyAsync(out->cells.data(), b.nodes, cells * sizeof(OctNode), cudaMemcpyDeviceToHost, s);
+            if (e != cudaSuccess)
+                return ctx_cuda_fail(ctx, e, "tree readback");
+        }
         return check_device_error(ctx);
     }
 

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "nbody_cuda.h"
@@ -30,7 +31,20 @@ namespace nbg
     };
     static_assert(sizeof(OctNode) == 64, "OctNode is one 64-byte record");
 
+    // Host copy of the last device tree (tree_export.cu turns it into reference nodes).
+    struct TreeSnapshot
+    {
+        size_t n = 0;                   // bodies
+        uint64_t build_id = 0;
+        BoxParams box{};
+        std::vector<OctNode> cells;     // cell 0 is the root cell (n >= 2)
+        std::vector<uint64_t> codes;    // sorted Morton codes
+        std::vector<float4> bodies;     // pos + mass in Morton order
+    };
+
     int bh_build(nbody_cuda* ctx, const nbody_step_params* p);
+    int bh_download(nbody_cuda* ctx, TreeSnapshot* out);
+    uint64_t bh_build_id(const nbody_cuda* ctx);    // 0 before the first build
     int bh_stats(nbody_cuda* ctx, unsigned long long out[3]);
     int bh_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* codes, uint32_t* order, double box[4]);
 }

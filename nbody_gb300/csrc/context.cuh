@@ -5,6 +5,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "nbody_cuda.h"
@@ -53,6 +54,10 @@ struct nbody_cuda
     bool origin_valid = false;
     nbg::PreciseState* precise = nullptr;
     nbg::BhState* bh = nullptr;
+
+    // The last tree in the reference's node layout (tree_export.cu), and the build it is of.
+    std::vector<unsigned char> tree_export;
+    uint64_t tree_export_id = 0;
 
     int force_variant = -1;     // pins the direct-sum (T, block) table entry when >= 0
     nbg::DirectPlan last_plan{};

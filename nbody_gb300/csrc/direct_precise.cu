@@ -465,7 +465,7 @@ namespace nbg
     __global__ void integrate_comp_kernel(float4* __restrict__ off, float4* __restrict__ cx, float4* __restrict__ cv,
                                           float4* __restrict__ pm, float4* __restrict__ vr, float* __restrict__ bodies,
                                           const float4* __restrict__ acc, const double* __restrict__ origin,
-                                          const int n, const float dt)
+                                          const int n, const float dt, const float size, const int wrap)
     {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
         if (i >= n)
@@ -490,12 +490,30 @@ namespace nbg
         kahan(o.x, c.x, __fmul_rn(v.x, dt));
         kahan(o.y, c.y, __fmul_rn(v.y, dt));
         kahan(o.z, c.z, __fmul_rn(v.z, dt));
+        double pos[3] = { origin[0] + ((double)o.x - (double)c.x), origin[1] + ((double)o.y - (double)c.y),
+                          origin[2] + ((double)o.z - (double)c.z) };
+        if (wrap && size > 0.f)
+        {
+            // the 3-torus of physics.h:50-58, applied to the compensated position in FP64;
+            // a wrapped body's offset and compensation are re-derived from the new position
+            const double s = size, half = 0.5 * s;
+            float* oo[3] = { &o.x, &o.y, &o.z };
+            float* cc[3] = { &c.x, &c.y, &c.z };
+            for (int a = 0; a < 3; ++a)
+                if (pos[a] < -half || pos[a] > half)
+                {
+                    pos[a] = fmod(fmod(pos[a] + half, s) + s, s) - half;
+                    const double r = pos[a] - origin[a];
+                    *oo[a] = (float)r;
+                    *cc[a] = (float)((double)*oo[a] - r);
+                }
+        }
         off[i] = o;
         cx[i] = c;
         cv[i] = w;
-        const float x = (float)(origin[0] + ((double)o.x - (double)c.x));
-        const float y = (float)(origin[1] + ((double)o.y - (double)c.y));
-        const float z = (float)(origin[2] + ((double)o.z - (double)c.z));
+        const float x = (float)pos[0];
+        const float y = (float)pos[1];
+        const float z = (float)pos[2];
         if (bodies)
         {
             float4* b = reinterpret_cast<float4*>(bodies) + static_cast<size_t>(i) * 3;
@@ -713,8 +731,6 @@ namespace nbg
 
     int precise_integrate(nbody_cuda* ctx, const nbody_step_params* p)
     {
-        if (p->wrap && p->size > 0.f)
-            return ctx_fail(ctx, NBODY_ERR_UNSUPPORTED, "the compensated integrator does not wrap; use FP32 precision with wrap");
         if (const int st = ensure_split_state(ctx))
             return st;
         if (ctx->pending_partials > 1)
@@ -731,7 +747,7 @@ namespace nbg
         PreciseState& s = *ctx->precise;
         integrate_comp_kernel<<<ceil_div(ctx->count, 256), 256, 0, ctx->stream>>>(
             s.off, s.cx, s.cv, ctx->pm, ctx->vr, ctx->layout == NBODY_LAYOUT_AOS ? ctx->bodies : nullptr, ctx->acc,
-            s.origin, static_cast<int>(ctx->count), p->dt);
+            s.origin, static_cast<int>(ctx->count), p->dt, p->size, p->wrap);
         ++ctx->launches;
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess)

@@ -21,6 +21,10 @@ PREC_FP32, PREC_COMPENSATED, PREC_FP64 = 0, 1, 2
 LAYOUT_SOA, LAYOUT_AOS = 0, 1
 READ_POSITIONS, READ_VELOCITIES, READ_ACCELERATIONS, READ_ALL = 1, 2, 4, 7
 
+# bh::Node (include/nbody/bhtree.h of the reference): bounds centre, size, com, mass, links
+NODE_DTYPE = np.dtype([("center", "<f4", 3), ("size", "<f4"), ("com", "<f4", 3), ("mass", "<f4"),
+                       ("next", "<u4"), ("children", "<u4"), ("pad", "<u4", 2)])
+
 # Every symbol include/nbody_cuda.h declares (checked by tests/test_boundary.py).
 EXPORTS = (
     "nbody_cuda_probe", "nbody_cuda_create", "nbody_cuda_destroy", "nbody_cuda_last_error",
@@ -32,6 +36,7 @@ EXPORTS = (
     "nbody_cuda_launch_count", "nbody_cuda_last_direct_config", "nbody_cuda_calibrate_fp32",
     "nbody_cuda_dev_accel_soa_noalloc", "nbody_cuda_bh_stats", "nbody_cuda_morton",
     "nbody_cuda_accel_sampled", "nbody_cuda_split_origin", "nbody_cuda_calibrate_fp64",
+    "nbody_cuda_tree_export",
 )
 
 
@@ -96,6 +101,7 @@ def lib() -> C.CDLL:
         "nbody_cuda_accel_sampled": ([vp, P, vp, sz, vp], C.c_int),
         "nbody_cuda_split_origin": ([vp, C.POINTER(C.c_double)], C.c_int),
         "nbody_cuda_calibrate_fp64": ([vp, C.POINTER(C.c_double)], C.c_int),
+        "nbody_cuda_tree_export": ([vp, vp, sz, C.POINTER(sz)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -230,6 +236,14 @@ class Context:
         t = np.ascontiguousarray(targets, np.int64)
         out = np.zeros((len(t), 3), np.float64)
         self.check(lib().nbody_cuda_accel_sampled(self.h, C.byref(p), _ptr(t), len(t), _ptr(out)))
+        return out
+
+    def tree_export(self) -> np.ndarray:
+        """The last Barnes-Hut tree as reference-layout nodes (48-byte records)."""
+        n = C.c_size_t()
+        self.check(lib().nbody_cuda_tree_export(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, NODE_DTYPE)
+        self.check(lib().nbody_cuda_tree_export(self.h, _ptr(out), n.value, C.byref(n)))
         return out
 
     def split_origin(self) -> np.ndarray:

@@ -425,6 +425,19 @@ void orc_tree_accel(const orc_tree* t, const float* bodies, const size_t n,
     }
 }
 
+/* Tree::apply over a node array given from outside (e.g. a tree exported by the device
+ * layer): the same walk as orc_tree_accel, bhtree.cpp:97-138. */
+void orc_nodes_accel(const orc_node* nodes, const size_t count, const float* bodies, const size_t n,
+                     const int64_t* targets, const size_t ntargets, const float theta, const float G,
+                     float* acc_out, uint64_t* interactions, const int nthreads)
+{
+    orc_tree t;
+    t.nodes = (orc_node*)nodes;
+    t.count = count;
+    t.cap = count;
+    orc_tree_accel(&t, bodies, n, targets, ntargets, theta, G, acc_out, interactions, nthreads);
+}
+
 /* CpuBarnesHutSolver::accelerate: cpu_barnes_hut.h:22-44 (acc written in place). */
 void orc_barnes_hut(float* bodies, const size_t n, const float size, const float theta,
                     const float G, const int nthreads, uint64_t* interactions)

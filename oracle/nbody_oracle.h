@@ -69,6 +69,11 @@ void orc_tree_accel(const orc_tree* t, const float* bodies, size_t n,
                     const int64_t* targets, size_t ntargets, float theta, float G,
                     float* acc_out, uint64_t* interactions, int nthreads);
 
+/* Tree::apply over an arbitrary node array in the reference layout (root at index 0). */
+void orc_nodes_accel(const orc_node* nodes, size_t count, const float* bodies, size_t n,
+                     const int64_t* targets, size_t ntargets, float theta, float G,
+                     float* acc_out, uint64_t* interactions, int nthreads);
+
 /* --- FP64 direct sum (no reference counterpart) ----------------------------------- */
 /* pos_mass: 4 floats per body (x, y, z, m). radius: per-body cutoff radius for
  * ORC_LAW_CUTOFF (may be NULL: 0). Compensated (Neumaier) double accumulation.

@@ -62,6 +62,7 @@ def lib():
         L.orc_tree_nodes.argtypes = [C.c_void_p]
         L.orc_tree_nodes.restype = C.c_void_p
         L.orc_tree_accel.argtypes = [C.c_void_p, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, _F, _U64, C.c_int]
+        L.orc_nodes_accel.argtypes = [C.c_void_p, _SZ, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, _F, _U64, C.c_int]
         L.orc_direct_f64.argtypes = [_F, _F, _SZ, C.c_double, C.c_double, C.c_int, _I64, _SZ, _D, _D, C.c_int]
         L.orc_direct_f64_pos.argtypes = [_D, _D, _SZ, C.c_double, C.c_double, _I64, _SZ, _D, C.c_int]
         L.orc_energy_f64.argtypes = [_D, _D, _D, _SZ, C.c_double, C.c_double, _D, _D, _D, C.c_int]
@@ -188,6 +189,20 @@ class Tree:
         lib().orc_tree_accel(self._t, _p(b, _F), len(b), _p(t, _I64), 0 if t is None else len(t),
                              theta, G, _p(out, _F), _p(inter, _U64), nthreads)
         return out, int(inter[0])
+
+
+def nodes_accel(nodes, bodies, theta, G, targets=None, nthreads=0):
+    """Tree::apply (bhtree.cpp:97-138) over a node array in the reference layout."""
+    nd = np.ascontiguousarray(nodes)
+    assert nd.dtype == NODE_DTYPE
+    b = _bodies(bodies)
+    t = None if targets is None else np.ascontiguousarray(targets, np.int64)
+    nt = len(b) if t is None else len(t)
+    out = np.zeros((nt, 3), np.float32)
+    inter = np.zeros(1, np.uint64)
+    lib().orc_nodes_accel(nd.ctypes.data_as(C.c_void_p), len(nd), _p(b, _F), len(b), _p(t, _I64),
+                          0 if t is None else len(t), theta, G, _p(out, _F), _p(inter, _U64), nthreads)
+    return out, int(inter[0])
 
 
 def direct_f64(pos_mass, G, eps2=0.0, law=LAW_SOFTENED, radius=None, targets=None, nthreads=0,

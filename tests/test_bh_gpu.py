@@ -214,3 +214,44 @@ def test_bh_update_steps(gpu):
         ref, _ = O.barnes_hut(ref, 10000.0, 0.5, 1.0)
         ref = O.integrate(ref, 1 / 120, 10000.0, True)
     assert np.abs(out[:, :3] - ref[:, :3]).max() < 1e-3
+
+
+def _cells(nodes):
+    """Non-empty nodes keyed by (centre, size): the tree's cells, independent of order."""
+    return {(tuple(n["center"]), float(n["size"])): (float(n["mass"]), tuple(n["com"]), int(n["children"] != 0))
+            for n in nodes if n["mass"] != 0}
+
+
+@pytest.mark.parametrize("fixture", ["cube_4096.npz", "disk_2048.npz"])
+def test_tree_export_is_the_reference_tree(gpu, fixture):
+    """nbody_cuda_tree_export gives the reference's octree: the same cells, node count,
+    masses, centres of mass (to rounding), and Tree::apply over it (oracle) gives the
+    reference's accelerations."""
+    g = golden(fixture)
+    b = g["bodies"]
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        ctx.accelerate(gpu.params(mode=gpu.MODE_NLOGN, theta=0.5, size=10000.0))
+        nodes = ctx.tree_export()
+    ref = O.ref_build_tree(b, 10000.0) if O.ref_available() else np.frombuffer(
+        golden("cube_4096.npz")["nodes"].tobytes(), dtype=O.NODE_DTYPE) if fixture == "cube_4096.npz" else None
+    if ref is None:
+        t = O.Tree(10000.0)
+        t.build(b, 10000.0)
+        ref = t.nodes()
+    assert len(nodes) == len(ref)
+    ours, theirs = _cells(nodes), _cells(ref)
+    assert ours.keys() == theirs.keys()
+    for k, (m, com, split) in theirs.items():
+        m2, com2, split2 = ours[k]
+        assert split == split2 and abs(m - m2) <= 1e-6 * abs(m)
+        assert np.allclose(com, com2, rtol=1e-5, atol=1e-3)
+    # links: every node's children block and next pointer are in range, root next = 0
+    assert nodes[0]["next"] == 0
+    assert np.all(nodes["children"] < len(nodes)) and np.all(nodes["next"] < len(nodes))
+    acc, inter = O.nodes_accel(nodes.view(O.NODE_DTYPE), b, 0.5, 1.0)
+    racc, rinter = O.nodes_accel(ref.view(O.NODE_DTYPE), b, 0.5, 1.0)
+    assert abs(inter - rinter) <= 0.01 * rinter
+    scale = term_scale(b)
+    err = np.linalg.norm(acc.astype(np.float64) - racc, axis=1) / scale
+    assert np.median(err) <= 1e-5 and (err > TOL).sum() <= len(b) // 500 + 2

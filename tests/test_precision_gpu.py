@@ -151,9 +151,6 @@ def test_precision_errors_reported(gpu):
     with gpu.Context() as ctx:
         ctx.upload_bodies(b)
         with pytest.raises(gpu.NbodyError) as e:
-            ctx.update(gpu.params(precision=gpu.PREC_COMPENSATED, wrap=True, size=1000.0, dt=0.01))
-        assert e.value.status == gpu.ERR_UNSUPPORTED
-        with pytest.raises(gpu.NbodyError) as e:
             ctx.accelerate(gpu.params(precision=gpu.PREC_FP64, mode=gpu.MODE_NLOGN))
         assert e.value.status == gpu.ERR_UNSUPPORTED
         with pytest.raises(gpu.NbodyError) as e:
@@ -161,6 +158,18 @@ def test_precision_errors_reported(gpu):
         assert e.value.status == gpu.ERR_INVALID
         ctx.accelerate(gpu.params(precision=gpu.PREC_COMPENSATED))     # still usable
         ctx.synchronize()
+
+
+def test_compensated_wrap_lands_where_reference_does(gpu):
+    """test_wrap.cpp:81-110 for the compensated integrator (wrap taken in FP64)."""
+    b = np.zeros((1, 12), np.float32)
+    b[0, :8] = (499, 0, 0, 1, 10, 0, 0, 1)
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        ctx.update(gpu.params(dt=1.0, G=0.0, size=1000.0, wrap=True, precision=gpu.PREC_COMPENSATED))
+        p = ctx.download_bodies()[0, :3]
+    ref = O.integrate(b, 1.0, 1000.0, True)[0, :3]
+    assert np.abs(p - ref).max() < 1e-3 and abs(p[0]) <= 500
 
 
 def test_bh_with_compensated_integration(gpu):
