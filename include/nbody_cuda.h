@@ -47,7 +47,10 @@ typedef enum nbody_status
 typedef enum nbody_mode
 {
     NBODY_MODE_N2 = 0,          /* direct summation (the reference's brute force) */
-    NBODY_MODE_NLOGN = 1        /* Barnes-Hut tree */
+    NBODY_MODE_NLOGN = 1,       /* Barnes-Hut tree */
+    NBODY_MODE_BATCHED = 2      /* direct summation within each system of the context's
+                                   system table (nbody_cuda_set_systems); no reference
+                                   counterpart */
 } nbody_mode;
 
 /* Force law. CUTOFF is the reference's (source/detail/physics.h:21-42): a pair
@@ -223,6 +226,37 @@ int nbody_cuda_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* cod
  * when nodes is NULL) and the total into *count. This is what Solver::tree() returns for a
  * tree-building variant (source/solvers/cpu_barnes_hut.h:46, sim.cpp:329-335). */
 int nbody_cuda_tree_export(nbody_cuda* ctx, void* nodes, size_t max_nodes, size_t* count);
+
+/* --- batched systems and graphs (no reference counterpart) ------------------------------- */
+
+/* Declare the context's bodies to be nsys independent systems: system s owns bodies
+ * [offsets[s], offsets[s+1]); offsets[0] = 0 and offsets[nsys] = the body count. Used by
+ * NBODY_MODE_BATCHED (one persistent launch sums every system) and by the energy
+ * diagnostics. Upload the concatenated bodies first. */
+int nbody_cuda_set_systems(nbody_cuda* ctx, const int64_t* offsets, size_t nsys);
+
+/* Time every batched kernel configuration (threads per target, targets per thread, inner
+ * unroll) on the current bodies and system table, keep the fastest for later batched steps
+ * and return its index in *best; times_ms (optional, ntimes entries) receives each
+ * configuration's accelerate time. Synchronous. */
+int nbody_cuda_batch_autotune(nbody_cuda* ctx, const nbody_step_params* p, double* times_ms,
+                              size_t ntimes, int* best);
+/* Number of batched configurations; describe one (index < 0: the active one); pin one. */
+int nbody_cuda_batch_config_count(void);
+int nbody_cuda_batch_config(const nbody_cuda* ctx, int index, int* threads_per_target,
+                            int* targets_per_thread, int* unroll);
+int nbody_cuda_batch_set_config(nbody_cuda* ctx, int index);
+
+/* FP64 diagnostics per system (one system covering every body when no table is set):
+ * out[5*s + 0..4] = kinetic energy, potential energy (softened with eps2 when p->law is
+ * SOFTENED, else unsoftened), momentum xyz. O(sum of N_s^2) FP64 work. Synchronous. */
+int nbody_cuda_system_energy(nbody_cuda* ctx, const nbody_step_params* p, double* out, size_t nsys);
+
+/* `steps` x update, with one step captured as a CUDA graph and replayed: the first step
+ * runs eagerly (it sets up every buffer), the step is captured once per parameter set,
+ * body count, stream and buffer generation, and replayed for the remaining steps. Results
+ * equal nbody_cuda_update's. The context's stream must not be the legacy default stream. */
+int nbody_cuda_update_graph(nbody_cuda* ctx, const nbody_step_params* p, int steps);
 
 /* --- precision forms --------------------------------------------------------------------- */
 

@@ -561,6 +561,8 @@ namespace nbg
             }
             if (n <= b.cap)
                 return NBODY_OK;
+            if (const int st = before_allocation(ctx))
+                return st;
             const size_t cap = std::max(n, b.cap + b.cap / 2);
             const size_t tb = std::max(sort_temp_bytes(cap), scan_temp_elems(cap + 1) * sizeof(double4));
             cudaError_t e = cudaSuccess;

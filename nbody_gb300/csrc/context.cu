@@ -13,6 +13,7 @@
 #include <new>
 #include <string>
 
+#include "batch.cuh"
 #include "bh.cuh"
 #include "common.cuh"
 #include "context.cuh"
@@ -86,7 +87,7 @@ namespace
             return fail(ctx, NBODY_ERR_INVALID, "unknown force law %d", p->law);
         if (p->law == NBODY_LAW_SOFTENED && !(p->eps2 > 0.f))
             return fail(ctx, NBODY_ERR_INVALID, "the softened law needs eps2 > 0 (got %g)", p->eps2);
-        if (p->mode != NBODY_MODE_N2 && p->mode != NBODY_MODE_NLOGN)
+        if (p->mode != NBODY_MODE_N2 && p->mode != NBODY_MODE_NLOGN && p->mode != NBODY_MODE_BATCHED)
             return fail(ctx, NBODY_ERR_INVALID, "unknown mode %d", p->mode);
         if (p->precision < NBODY_PREC_FP32 || p->precision > NBODY_PREC_FP64)
             return fail(ctx, NBODY_ERR_INVALID, "unknown precision %d", p->precision);
@@ -109,12 +110,22 @@ namespace nbg
         return cuda_fail(ctx, e, what);
     }
 
+    int before_allocation(nbody_cuda* ctx)
+    {
+        if (ctx->capturing)
+            return fail(ctx, NBODY_ERR_UNSUPPORTED, "a device buffer would grow during graph capture");
+        if (fault_injected("alloc"))
+            return fail(ctx, NBODY_ERR_ALLOC, "injected allocation failure (NBODY_CUDA_FAULT=alloc)");
+        ++ctx->generation;
+        return NBODY_OK;
+    }
+
     int ensure_scratch(nbody_cuda* ctx, const size_t bytes)
     {
         if (bytes <= ctx->scratch_bytes)
             return NBODY_OK;
-        if (fault_injected("alloc"))
-            return fail(ctx, NBODY_ERR_ALLOC, "injected allocation failure (NBODY_CUDA_FAULT=alloc)");
+        if (const int st = before_allocation(ctx))
+            return st;
         if (ctx->scratch)
             cudaFreeAsync(ctx->scratch, ctx->stream);
         ctx->scratch = nullptr;
@@ -227,6 +238,9 @@ void nbody_cuda_destroy(nbody_cuda* ctx)
         cudaStreamSynchronize(ctx->stream);
     release_bh(ctx);
     release_precise(ctx);
+    release_batch(ctx);
+    if (ctx->graph)
+        cudaGraphExecDestroy(ctx->graph);
     cudaFree(ctx->pm);
     cudaFree(ctx->vr);
     cudaFree(ctx->acc);
@@ -267,6 +281,7 @@ int nbody_cuda_set_stream(nbody_cuda* ctx, void* stream)
         cudaStreamWaitEvent(s, ev, 0);
         cudaEventDestroy(ev);
         ctx->stream = s;
+        ++ctx->generation;
     }
     return NBODY_OK;
 }
@@ -297,8 +312,8 @@ int nbody_cuda_reserve(nbody_cuda* ctx, const size_t n)
         return fail(ctx, NBODY_ERR_INVALID, "body count %zu exceeds this build's limit", n);
     if (n <= ctx->cap)
         return NBODY_OK;
-    if (fault_injected("alloc"))
-        return fail(ctx, NBODY_ERR_ALLOC, "injected allocation failure (NBODY_CUDA_FAULT=alloc)");
+    if (const int st = before_allocation(ctx))
+        return st;
     // Grow-only with headroom (Buffer::reserve, gpu.h:101-103); contents move with it.
     const size_t cap = std::max(n, ctx->cap + ctx->cap / 2);
     auto grow = [&](float4** p, const size_t per_body) -> int {
@@ -395,6 +410,8 @@ namespace
     {
         if (n <= ctx->aos_stage_cap)
             return NBODY_OK;
+        if (const int st = before_allocation(ctx))
+            return st;
         cudaFreeAsync(ctx->aos_stage, ctx->stream);
         ctx->aos_stage = nullptr;
         ctx->aos_stage_cap = 0;
@@ -410,6 +427,8 @@ int nbody_cuda_upload_bodies(nbody_cuda* ctx, const void* bodies, const size_t n
         return ctx ? fail(ctx, NBODY_ERR_INVALID, "null bodies") : NBODY_ERR_INVALID;
     if (const int st = nbody_cuda_reserve(ctx, n))
         return st;
+    if (n != ctx->count)
+        ++ctx->generation;      // the body count is an argument of captured launches
     ctx->count = n;
     ctx->origin_valid = false;
     if (!n)
@@ -483,6 +502,8 @@ int nbody_cuda_upload_soa(nbody_cuda* ctx, const float* pos_mass, const float* v
         return fail(ctx, NBODY_ERR_INVALID, "split-stream upload on an interleaved context");
     if (const int st = nbody_cuda_reserve(ctx, n))
         return st;
+    if (n != ctx->count)
+        ++ctx->generation;      // the body count is an argument of captured launches
     ctx->count = n;
     ctx->origin_valid = false;
     int st = NBODY_OK;
@@ -573,6 +594,8 @@ namespace
 
     int accelerate_impl(nbody_cuda* ctx, const nbody_step_params* p, const bool fuse_with_integrate)
     {
+        if (p->mode == NBODY_MODE_BATCHED)
+            return batch_accelerate(ctx, p);
         if (p->precision == NBODY_PREC_COMPENSATED || p->precision == NBODY_PREC_FP64)
             return precise_accelerate(ctx, p);
         if (p->mode == NBODY_MODE_NLOGN)
@@ -653,6 +676,133 @@ int nbody_cuda_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* cod
     if (const int st = check_params(ctx, p))
         return st;
     return bh_morton(ctx, p, codes, order, box);
+}
+
+int nbody_cuda_set_systems(nbody_cuda* ctx, const int64_t* offsets, size_t nsys)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    return batch_set_systems(ctx, offsets, nsys);
+}
+
+int nbody_cuda_batch_autotune(nbody_cuda* ctx, const nbody_step_params* p, double* times_ms, size_t ntimes, int* best)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    std::vector<double> t(static_cast<size_t>(batch_config_count()), 0.0);
+    const int st = batch_autotune(ctx, p, t.data(), best);
+    if (times_ms)
+        for (size_t i = 0; i < ntimes && i < t.size(); ++i)
+            times_ms[i] = t[i];
+    return st;
+}
+
+int nbody_cuda_batch_config_count(void) { return batch_config_count(); }
+
+int nbody_cuda_batch_config(const nbody_cuda* ctx, int index, int* tpt, int* t, int* unroll)
+{
+    if (index < 0)
+        index = ctx ? batch_get_config(ctx) : 0;
+    if (index >= batch_config_count())
+        return NBODY_ERR_INVALID;
+    int a = 0, b = 0, c = 0;
+    batch_config_describe(index, &a, &b, &c);
+    if (tpt) *tpt = a;
+    if (t) *t = b;
+    if (unroll) *unroll = c;
+    return NBODY_OK;
+}
+
+int nbody_cuda_batch_set_config(nbody_cuda* ctx, int index)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    return batch_set_config(ctx, index);
+}
+
+int nbody_cuda_system_energy(nbody_cuda* ctx, const nbody_step_params* p, double* out, size_t nsys)
+{
+    if (!ctx || !out)
+        return NBODY_ERR_INVALID;
+    if (!p)
+        return fail(ctx, NBODY_ERR_INVALID, "null step parameters");
+    const size_t have = std::max<size_t>(1, batch_system_count(ctx));
+    if (nsys < have)
+        return fail(ctx, NBODY_ERR_INVALID, "output holds %zu systems, the table has %zu", nsys, have);
+    nbody_step_params q = *p;
+    if (q.law != NBODY_LAW_SOFTENED)
+        q.eps2 = 0.f;
+    return batch_energy(ctx, &q, out);
+}
+
+int nbody_cuda_update_graph(nbody_cuda* ctx, const nbody_step_params* p, const int steps)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    if (steps < 0)
+        return fail(ctx, NBODY_ERR_INVALID, "negative step count");
+    if (!ctx->count || steps == 0)
+        return NBODY_OK;
+    // The first step runs eagerly: it grows every buffer the step needs, so nothing
+    // allocates while the step is captured.
+    if (const int st = nbody_cuda_update(ctx, p, 1))
+        return st;
+    if (steps == 1)
+        return NBODY_OK;
+    const bool stale = !ctx->graph || ctx->graph_generation != ctx->generation || ctx->graph_count != ctx->count
+                       || ctx->graph_stream != ctx->stream
+                       || std::memcmp(&ctx->graph_params, p, sizeof *p) != 0;
+    if (stale)
+    {
+        if (ctx->graph)
+            cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+        const uint64_t gen = ctx->generation;
+        const uint64_t launches_before = ctx->launches;
+        NBG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
+        ctx->capturing = true;
+        int st = accelerate_impl(ctx, p, true);
+        if (st == NBODY_OK)
+            st = integrate_impl(ctx, p);
+        ctx->capturing = false;
+        // captured, not run: count the kernels once per replay instead
+        ctx->graph_launches = ctx->launches - launches_before;
+        ctx->launches = launches_before;
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        if (st != NBODY_OK || e != cudaSuccess || gen != ctx->generation)
+        {
+            if (g)
+                cudaGraphDestroy(g);
+            cudaGetLastError();
+            if (st != NBODY_OK)
+                return st;
+            return e != cudaSuccess ? cuda_fail(ctx, e, "graph capture")
+                                    : fail(ctx, NBODY_ERR_CUDA, "buffers changed during graph capture");
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&ctx->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess)
+        {
+            ctx->graph = nullptr;
+            return cuda_fail(ctx, ie, "graph instantiate");
+        }
+        ctx->graph_generation = ctx->generation;
+        ctx->graph_count = ctx->count;
+        ctx->graph_stream = ctx->stream;
+        ctx->graph_params = *p;
+    }
+    for (int s = 1; s < steps; ++s)
+    {
+        NBG_CUDA(ctx, cudaGraphLaunch(ctx->graph, ctx->stream), "graph launch");
+        ctx->launches += ctx->graph_launches;
+    }
+    ctx->tree_export_id = 0;    // replays rebuilt the tree without the host noticing
+    return NBODY_OK;
 }
 
 int nbody_cuda_accel_sampled(nbody_cuda* ctx, const nbody_step_params* p, const int64_t* targets, size_t nt,

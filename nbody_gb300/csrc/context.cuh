@@ -15,6 +15,7 @@ namespace nbg
 {
     struct BhState;         // bh.cu
     struct PreciseState;    // direct_precise.cu
+    struct BatchState;      // batch.cu
 }
 
 struct nbody_cuda
@@ -55,6 +56,19 @@ struct nbody_cuda
     nbg::PreciseState* precise = nullptr;
     nbg::BhState* bh = nullptr;
 
+    nbg::BatchState* batch = nullptr;   // system table + batched work lists (batch.cu)
+
+    // Bumped whenever a device buffer moves or a kernel argument baked into a captured
+    // graph changes (uploads, growth, system tables, stream switches).
+    uint64_t generation = 0;
+    bool capturing = false;             // inside nbody_cuda_update_graph's capture: no allocation
+    cudaGraphExec_t graph = nullptr;
+    uint64_t graph_launches = 0;        // kernels in one replay of the captured step
+    nbody_step_params graph_params{};
+    uint64_t graph_generation = 0;
+    size_t graph_count = 0;
+    cudaStream_t graph_stream = nullptr;
+
     // The last tree in the reference's node layout (tree_export.cu), and the build it is of.
     std::vector<unsigned char> tree_export;
     uint64_t tree_export_id = 0;
@@ -72,6 +86,9 @@ namespace nbg
     int ctx_fail(nbody_cuda* ctx, int status, const char* msg);
     int ctx_cuda_fail(nbody_cuda* ctx, cudaError_t e, const char* what);
     int ensure_scratch(nbody_cuda* ctx, size_t bytes);
+    // Every growth of a device buffer goes through here: refused during graph capture (the
+    // pointers a graph holds must stay valid), and it retires any captured graph.
+    int before_allocation(nbody_cuda* ctx);
     int check_device_error(nbody_cuda* ctx);
 
     // direct_precise.cu

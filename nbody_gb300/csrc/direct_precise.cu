@@ -568,6 +568,8 @@ namespace nbg
             }
             if (n <= s.cap)
                 return NBODY_OK;
+            if (const int st = before_allocation(ctx))
+                return st;
             const size_t cap = std::max(n, s.cap + s.cap / 2);
             cudaError_t e = regrow(&s.off, cap, st);
             if (e == cudaSuccess) e = regrow(&s.cx, cap, st);

@@ -15,7 +15,7 @@ LIB_PATH = Path(__file__).resolve().parent / "lib" / "libnbody_cuda.so"
 
 # status codes (nbody_status)
 OK, ERR_INVALID, ERR_NO_DEVICE, ERR_CUDA, ERR_ALLOC, ERR_TIMEOUT, ERR_UNSUPPORTED = range(7)
-MODE_N2, MODE_NLOGN = 0, 1
+MODE_N2, MODE_NLOGN, MODE_BATCHED = 0, 1, 2
 LAW_CUTOFF, LAW_SOFTENED = 0, 1
 PREC_FP32, PREC_COMPENSATED, PREC_FP64 = 0, 1, 2
 LAYOUT_SOA, LAYOUT_AOS = 0, 1
@@ -36,7 +36,9 @@ EXPORTS = (
     "nbody_cuda_launch_count", "nbody_cuda_last_direct_config", "nbody_cuda_calibrate_fp32",
     "nbody_cuda_dev_accel_soa_noalloc", "nbody_cuda_bh_stats", "nbody_cuda_morton",
     "nbody_cuda_accel_sampled", "nbody_cuda_split_origin", "nbody_cuda_calibrate_fp64",
-    "nbody_cuda_tree_export",
+    "nbody_cuda_tree_export", "nbody_cuda_set_systems", "nbody_cuda_batch_autotune",
+    "nbody_cuda_batch_config_count", "nbody_cuda_batch_config", "nbody_cuda_batch_set_config",
+    "nbody_cuda_system_energy", "nbody_cuda_update_graph",
 )
 
 
@@ -102,6 +104,13 @@ def lib() -> C.CDLL:
         "nbody_cuda_split_origin": ([vp, C.POINTER(C.c_double)], C.c_int),
         "nbody_cuda_calibrate_fp64": ([vp, C.POINTER(C.c_double)], C.c_int),
         "nbody_cuda_tree_export": ([vp, vp, sz, C.POINTER(sz)], C.c_int),
+        "nbody_cuda_set_systems": ([vp, vp, sz], C.c_int),
+        "nbody_cuda_batch_autotune": ([vp, P, vp, sz, C.POINTER(C.c_int)], C.c_int),
+        "nbody_cuda_batch_config_count": ([], C.c_int),
+        "nbody_cuda_batch_config": ([vp, C.c_int] + [C.POINTER(C.c_int)] * 3, C.c_int),
+        "nbody_cuda_batch_set_config": ([vp, C.c_int], C.c_int),
+        "nbody_cuda_system_energy": ([vp, P, vp, sz], C.c_int),
+        "nbody_cuda_update_graph": ([vp, P, C.c_int], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -237,6 +246,36 @@ class Context:
         out = np.zeros((len(t), 3), np.float64)
         self.check(lib().nbody_cuda_accel_sampled(self.h, C.byref(p), _ptr(t), len(t), _ptr(out)))
         return out
+
+    # --- batched systems and graphs ------------------------------------------------------------
+    def set_systems(self, offsets):
+        o = np.ascontiguousarray(offsets, np.int64)
+        self.nsys = len(o) - 1
+        self.check(lib().nbody_cuda_set_systems(self.h, _ptr(o), len(o) - 1))
+
+    def batch_autotune(self, p: StepParams):
+        n = int(lib().nbody_cuda_batch_config_count())
+        times = np.zeros(n, np.float64)
+        best = C.c_int()
+        self.check(lib().nbody_cuda_batch_autotune(self.h, C.byref(p), _ptr(times), n, C.byref(best)))
+        return best.value, times
+
+    def batch_config(self, index: int = -1) -> dict:
+        v = [C.c_int() for _ in range(3)]
+        self.check(lib().nbody_cuda_batch_config(self.h, index, *[C.byref(x) for x in v]))
+        return dict(zip(("threads_per_target", "targets_per_thread", "unroll"), (x.value for x in v)))
+
+    def batch_set_config(self, index: int):
+        self.check(lib().nbody_cuda_batch_set_config(self.h, index))
+
+    def system_energy(self, p: StepParams, nsys: int | None = None) -> np.ndarray:
+        n = nsys or getattr(self, "nsys", 1) or 1
+        out = np.zeros((n, 5), np.float64)
+        self.check(lib().nbody_cuda_system_energy(self.h, C.byref(p), _ptr(out), n))
+        return out
+
+    def update_graph(self, p: StepParams, steps: int):
+        self.check(lib().nbody_cuda_update_graph(self.h, C.byref(p), steps))
 
     def tree_export(self) -> np.ndarray:
         """The last Barnes-Hut tree as reference-layout nodes (48-byte records)."""
