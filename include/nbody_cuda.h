@@ -227,6 +227,21 @@ int nbody_cuda_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* cod
  * tree-building variant (source/solvers/cpu_barnes_hut.h:46, sim.cpp:329-335). */
 int nbody_cuda_tree_export(nbody_cuda* ctx, void* nodes, size_t max_nodes, size_t* count);
 
+/* --- direct-sum kernel shapes ---------------------------------------------------------------- */
+
+/* Number of instantiated direct-sum kernel shapes; describe one (targets per thread, threads
+ * per CTA, packed FP32x2 arithmetic or scalar); pin one for this context (index < 0 returns
+ * to the size-based choice). */
+int nbody_cuda_direct_variant_count(void);
+int nbody_cuda_direct_variant(int index, int* targets_per_thread, int* block, int* packed);
+int nbody_cuda_set_direct_variant(nbody_cuda* ctx, int index);
+
+/* Time every direct-sum kernel shape on the current bodies (FP32, p->law), pin the fastest
+ * and return its index in *best; times_ms (optional, ntimes entries) receives each shape's
+ * accelerate time. Synchronous. */
+int nbody_cuda_direct_autotune(nbody_cuda* ctx, const nbody_step_params* p, double* times_ms,
+                               size_t ntimes, int* best);
+
 /* --- batched systems and graphs (no reference counterpart) ------------------------------- */
 
 /* Declare the context's bodies to be nsys independent systems: system s owns bodies

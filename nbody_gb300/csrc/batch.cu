@@ -274,6 +274,8 @@ namespace nbg
                 cfg<2, 2, 2>(), cfg<2, 2, 4>(), cfg<2, 4, 2>(), cfg<2, 4, 4>(),
                 cfg<4, 2, 2>(), cfg<4, 2, 4>(), cfg<4, 4, 2>(), cfg<4, 4, 4>(),
                 cfg<8, 2, 2>(), cfg<8, 2, 4>(), cfg<8, 4, 2>(), cfg<8, 4, 4>(),
+                cfg<2, 8, 2>(), cfg<4, 8, 2>(), cfg<8, 8, 2>(), cfg<8, 8, 4>(),
+                cfg<16, 4, 4>(), cfg<16, 8, 2>(),
             };
             return c;
         }

@@ -119,10 +119,36 @@ namespace nbg
             part[blockIdx.x * 6 + threadIdx.x] = red[threadIdx.x][0];
     }
 
-    __global__ void box_final_kernel(const double* __restrict__ part, const int nparts, const int mode,
-                                     const float size, BoxParams* __restrict__ box)
+    __global__ void __launch_bounds__(256) box_final_kernel(const double* __restrict__ part, const int nparts,
+                                                            const int mode, const float size,
+                                                            BoxParams* __restrict__ box)
     {
-        if (threadIdx.x != 0 || blockIdx.x != 0)
+        // one block folds the per-block partials (a strided pass, then a tree)
+        __shared__ double red[6][256];
+        double l[3] = { INFINITY, INFINITY, INFINITY }, h[3] = { -INFINITY, -INFINITY, -INFINITY };
+        for (int k = threadIdx.x; k < nparts; k += blockDim.x)
+            for (int a = 0; a < 3; ++a)
+            {
+                l[a] = fmin(l[a], part[k * 6 + a]);
+                h[a] = fmax(h[a], part[k * 6 + 3 + a]);
+            }
+        for (int a = 0; a < 3; ++a)
+        {
+            red[a][threadIdx.x] = l[a];
+            red[3 + a][threadIdx.x] = h[a];
+        }
+        __syncthreads();
+        for (int s = blockDim.x / 2; s > 0; s >>= 1)
+        {
+            if (threadIdx.x < s)
+                for (int a = 0; a < 3; ++a)
+                {
+                    red[a][threadIdx.x] = fmin(red[a][threadIdx.x], red[a][threadIdx.x + s]);
+                    red[3 + a][threadIdx.x] = fmax(red[3 + a][threadIdx.x], red[3 + a][threadIdx.x + s]);
+                }
+            __syncthreads();
+        }
+        if (threadIdx.x != 0)
             return;
         BoxParams b;
         if (mode == 0)
@@ -138,13 +164,8 @@ namespace nbg
         }
         else
         {
-            double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
-            for (int k = 0; k < nparts; ++k)
-                for (int a = 0; a < 3; ++a)
-                {
-                    lo[a] = fmin(lo[a], part[k * 6 + a]);
-                    hi[a] = fmax(hi[a], part[k * 6 + 3 + a]);
-                }
+            const double lo[3] = { red[0][0], red[1][0], red[2][0] };
+            const double hi[3] = { red[3][0], red[4][0], red[5][0] };
             double ext = 0.0;
             for (int a = 0; a < 3; ++a)
                 ext = fmax(ext, hi[a] - lo[a]);
@@ -633,7 +654,7 @@ namespace nbg
             bbox_partial_kernel<<<kBboxBlocks, 256, 0, s>>>(src, stride, ni, b.bbox_part);
             ++L;
         }
-        box_final_kernel<<<1, 32, 0, s>>>(b.bbox_part, auto_box ? kBboxBlocks : 0, auto_box ? 1 : 0, p->size, b.box);
+        box_final_kernel<<<1, 256, 0, s>>>(b.bbox_part, auto_box ? kBboxBlocks : 0, auto_box ? 1 : 0, p->size, b.box);
         ++L;
         morton_kernel<<<blocks, 256, 0, s>>>(src, stride, ni, b.box, b.keys[0], b.vals[0]);
         ++L;

@@ -678,6 +678,92 @@ int nbody_cuda_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* cod
     return bh_morton(ctx, p, codes, order, box);
 }
 
+int nbody_cuda_direct_variant_count(void) { return direct_variant_count(); }
+
+int nbody_cuda_direct_variant(const int index, int* T, int* block, int* packed)
+{
+    if (index < 0 || index >= direct_variant_count())
+        return NBODY_ERR_INVALID;
+    int a = 0, b = 0, c = 0;
+    direct_variant_describe(index, &a, &b, &c);
+    if (T) *T = a;
+    if (block) *block = b;
+    if (packed) *packed = c;
+    return NBODY_OK;
+}
+
+int nbody_cuda_set_direct_variant(nbody_cuda* ctx, const int index)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (index >= direct_variant_count())
+        return fail(ctx, NBODY_ERR_INVALID, "no direct-sum kernel shape %d", index);
+    ctx->force_variant = index < 0 ? -1 : index;
+    return NBODY_OK;
+}
+
+int nbody_cuda_direct_autotune(nbody_cuda* ctx, const nbody_step_params* p, double* times_ms, size_t ntimes,
+                               int* best)
+{
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    if (!ctx->count)
+        return fail(ctx, NBODY_ERR_INVALID, "no bodies to tune on");
+    nbody_step_params q = *p;
+    q.mode = NBODY_MODE_N2;
+    q.precision = NBODY_PREC_FP32;
+    cudaEvent_t e0, e1;
+    NBG_CUDA(ctx, cudaEventCreate(&e0), "event create");
+    NBG_CUDA(ctx, cudaEventCreate(&e1), "event create");
+    // one untimed launch first, so the clocks are up before the first shape is timed
+    ctx->force_variant = -1;
+    if (const int st = direct_accel(ctx, &q, false))
+    {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return st;
+    }
+    int best_i = 0;
+    float best_ms = 1e30f;
+    for (int i = 0; i < direct_variant_count(); ++i)
+    {
+        ctx->force_variant = i;
+        float ms_best = 1e30f;
+        for (int rep = 0; rep < 2; ++rep)
+        {
+            cudaEventRecord(e0, ctx->stream);
+            const int st = direct_accel(ctx, &q, false);
+            cudaEventRecord(e1, ctx->stream);
+            if (st != NBODY_OK)
+            {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                ctx->force_variant = -1;
+                return st;
+            }
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms_best = std::min(ms_best, ms);
+        }
+        if (times_ms && static_cast<size_t>(i) < ntimes)
+            times_ms[i] = ms_best;
+        if (ms_best < best_ms)
+        {
+            best_ms = ms_best;
+            best_i = i;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->force_variant = best_i;
+    if (best)
+        *best = best_i;
+    return check_device_error(ctx);
+}
+
 int nbody_cuda_set_systems(nbody_cuda* ctx, const int64_t* offsets, size_t nsys)
 {
     if (!ctx)

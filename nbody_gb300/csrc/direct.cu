@@ -25,13 +25,49 @@
 
 namespace nbg
 {
-    // One source (sx, sy, sz, sm) applied to two targets held as negated positions.
+    // One source (sx, sy, sz, sm) applied to two targets held as negated positions, as
+    // scalar FP32 instructions (the same arithmetic; for comparison with the packed form).
     template <int LAW>
+    __device__ __forceinline__ void interact2_scalar(const float2 sx, const float2 sy, const float2 sz,
+                                                     const float2 sm, const float2 nx, const float2 ny,
+                                                     const float2 nz, const float2 lim, float2& ax,
+                                                     float2& ay, float2& az)
+    {
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+        {
+            const float dx = (h ? sx.y : sx.x) + (h ? nx.y : nx.x);
+            const float dy = (h ? sy.y : sy.x) + (h ? ny.y : ny.x);
+            const float dz = (h ? sz.y : sz.x) + (h ? nz.y : nz.x);
+            const float l = h ? lim.y : lim.x;
+            float r2 = (LAW == NBODY_LAW_SOFTENED) ? fmaf(dx, dx, l) : dx * dx;
+            r2 = fmaf(dy, dy, r2);
+            r2 = fmaf(dz, dz, r2);
+            float inv = rsqrt_sfu(r2);
+            if (LAW == NBODY_LAW_CUTOFF)
+                inv = r2 > l ? inv : 0.f;
+            const float s = ((h ? sm.y : sm.x) * inv) * (inv * inv);
+            float& x = h ? ax.y : ax.x;
+            float& y = h ? ay.y : ay.x;
+            float& z = h ? az.y : az.x;
+            x = fmaf(dx, s, x);
+            y = fmaf(dy, s, y);
+            z = fmaf(dz, s, z);
+        }
+    }
+
+    // One source (sx, sy, sz, sm) applied to two targets held as negated positions.
+    template <int LAW, bool PACKED = true>
     __device__ __forceinline__ void interact2(const float2 sx, const float2 sy, const float2 sz,
                                               const float2 sm, const float2 nx, const float2 ny,
                                               const float2 nz, const float2 lim, float2& ax,
                                               float2& ay, float2& az)
     {
+        if (!PACKED)
+        {
+            interact2_scalar<LAW>(sx, sy, sz, sm, nx, ny, nz, lim, ax, ay, az);
+            return;
+        }
         const float2 dx = add2(sx, nx);
         const float2 dy = add2(sy, ny);
         const float2 dz = add2(sz, nz);
@@ -61,7 +97,7 @@ namespace nbg
         static constexpr int kRec = AOS ? 3 : 1;
     };
 
-    template <int T, int BLOCK, int TILE, int STAGES, int LAW, bool AOS>
+    template <int T, int BLOCK, int TILE, int STAGES, int LAW, bool AOS, bool PACKED = true>
     __global__ void __launch_bounds__(BLOCK, (T >= 8 ? 2 : 3))
     direct_fp32_kernel(const float4* __restrict__ src,        // pos_mass (SoA) or Body (AoS)
                        const float4* __restrict__ vel_radius, // SoA radius source (CUTOFF)
@@ -157,7 +193,7 @@ namespace nbg
                 const float2 sx = f2(s.x), sy = f2(s.y), sz = f2(s.z), sm = f2(m);
 #pragma unroll
                 for (int p = 0; p < P; ++p)
-                    interact2<LAW>(sx, sy, sz, sm, nx[p], ny[p], nz[p], lim[p], ax[p], ay[p], az[p]);
+                    interact2<LAW, PACKED>(sx, sy, sz, sm, nx[p], ny[p], nz[p], lim[p], ax[p], ay[p], az[p]);
             }
             __syncthreads();
             if (tid == 0 && t + STAGES < ntiles)
@@ -242,29 +278,39 @@ namespace nbg
         struct Variant
         {
             int T, block;
+            bool packed;
             KernelFn fn[2][2];  // [law][aos]
         };
 
-        template <int T, int B>
+        constexpr int kPlanned = 4;
+
+        template <int T, int B, bool PACKED = true>
         Variant make_variant()
         {
             Variant v;
             v.T = T;
             v.block = B;
-            v.fn[0][0] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_CUTOFF, false>;
-            v.fn[0][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_CUTOFF, true>;
-            v.fn[1][0] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, false>;
-            v.fn[1][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, true>;
+            v.packed = PACKED;
+            v.fn[0][0] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_CUTOFF, false, PACKED>;
+            v.fn[0][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_CUTOFF, true, PACKED>;
+            v.fn[1][0] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, false, PACKED>;
+            v.fn[1][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, true, PACKED>;
             return v;
         }
 
         const Variant* variants(int* count)
         {
+            // The first kPlanned entries are what plan_direct chooses between by size; the
+            // rest are further shapes the direct-sum autotuner can time and pin.
             static const Variant v[] = {
                 make_variant<8, 256>(),
                 make_variant<4, 256>(),
                 make_variant<4, 128>(),
                 make_variant<2, 64>(),
+                make_variant<8, 256, false>(),
+                make_variant<8, 128>(),
+                make_variant<6, 128>(),
+                make_variant<12, 128>(),
             };
             *count = static_cast<int>(sizeof(v) / sizeof(v[0]));
             return v;
@@ -305,7 +351,7 @@ namespace nbg
         else
         {
             // Largest register block whose (target blocks x max chunks) fills the GPU.
-            for (int k = 0; k < nv; ++k)
+            for (int k = 0; k < kPlanned; ++k)
             {
                 const size_t per = static_cast<size_t>(vs[k].T) * vs[k].block;
                 const size_t tb = (n + per - 1) / per;
@@ -318,7 +364,7 @@ namespace nbg
                 }
             }
             if (chosen < 0)
-                chosen = nv - 1;
+                chosen = kPlanned - 1;
         }
         const Variant& v = vs[chosen];
         const size_t per = static_cast<size_t>(v.T) * v.block;
@@ -379,6 +425,22 @@ namespace nbg
         if (e != cudaSuccess || plan.jsplit <= 1 || !reduce)
             return e;
         return launch_reduce(scratch, plan.jsplit, n, acc, plan.aos ? body_out : nullptr, stream, launches);
+    }
+
+    int direct_variant_count()
+    {
+        int nv = 0;
+        variants(&nv);
+        return nv;
+    }
+
+    void direct_variant_describe(const int i, int* T, int* block, int* packed)
+    {
+        int nv = 0;
+        const Variant* vs = variants(&nv);
+        *T = vs[i].T;
+        *block = vs[i].block;
+        *packed = vs[i].packed ? 1 : 0;
     }
 
     cudaError_t launch_reduce(const float4* scratch, const int jsplit, const int n, float4* acc,

@@ -24,6 +24,10 @@ namespace nbg
     // Pick a launch shape for n bodies. force_variant >= 0 pins the (T, block) entry.
     DirectPlan plan_direct(size_t n, int law, bool aos, int force_variant = -1);
 
+    // The instantiated kernel shapes: targets per thread, threads per CTA, packed FP32x2 or not.
+    int direct_variant_count();
+    void direct_variant_describe(int i, int* T, int* block, int* packed);
+
     // Queue the accelerate. src is pos_mass (SoA) or the Body array viewed as float4
     // (AoS). Results: acc (SoA) or Body::acc in body_out (AoS). scratch must hold
     // plan.jsplit * n float4 when plan.jsplit > 1; with reduce == false the partials are

@@ -38,7 +38,8 @@ EXPORTS = (
     "nbody_cuda_accel_sampled", "nbody_cuda_split_origin", "nbody_cuda_calibrate_fp64",
     "nbody_cuda_tree_export", "nbody_cuda_set_systems", "nbody_cuda_batch_autotune",
     "nbody_cuda_batch_config_count", "nbody_cuda_batch_config", "nbody_cuda_batch_set_config",
-    "nbody_cuda_system_energy", "nbody_cuda_update_graph",
+    "nbody_cuda_system_energy", "nbody_cuda_update_graph", "nbody_cuda_direct_variant_count",
+    "nbody_cuda_direct_variant", "nbody_cuda_set_direct_variant", "nbody_cuda_direct_autotune",
 )
 
 
@@ -111,6 +112,10 @@ def lib() -> C.CDLL:
         "nbody_cuda_batch_set_config": ([vp, C.c_int], C.c_int),
         "nbody_cuda_system_energy": ([vp, P, vp, sz], C.c_int),
         "nbody_cuda_update_graph": ([vp, P, C.c_int], C.c_int),
+        "nbody_cuda_direct_variant_count": ([], C.c_int),
+        "nbody_cuda_direct_variant": ([C.c_int] + [C.POINTER(C.c_int)] * 3, C.c_int),
+        "nbody_cuda_set_direct_variant": ([vp, C.c_int], C.c_int),
+        "nbody_cuda_direct_autotune": ([vp, P, vp, sz, C.POINTER(C.c_int)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -273,6 +278,25 @@ class Context:
         out = np.zeros((n, 5), np.float64)
         self.check(lib().nbody_cuda_system_energy(self.h, C.byref(p), _ptr(out), n))
         return out
+
+    # --- direct-sum kernel shapes ----------------------------------------------------------
+    @staticmethod
+    def direct_variant(index: int) -> dict:
+        v = [C.c_int() for _ in range(3)]
+        st = lib().nbody_cuda_direct_variant(index, *[C.byref(x) for x in v])
+        if st != OK:
+            raise NbodyError(st, f"no direct-sum kernel shape {index}")
+        return dict(zip(("targets_per_thread", "block", "packed"), (x.value for x in v)))
+
+    def set_direct_variant(self, index: int):
+        self.check(lib().nbody_cuda_set_direct_variant(self.h, index))
+
+    def direct_autotune(self, p: StepParams):
+        n = int(lib().nbody_cuda_direct_variant_count())
+        times = np.zeros(n, np.float64)
+        best = C.c_int()
+        self.check(lib().nbody_cuda_direct_autotune(self.h, C.byref(p), _ptr(times), n, C.byref(best)))
+        return best.value, times
 
     def update_graph(self, p: StepParams, steps: int):
         self.check(lib().nbody_cuda_update_graph(self.h, C.byref(p), steps))

@@ -20,13 +20,37 @@ def main(argv=None) -> int:
 
     ap = argparse.ArgumentParser()
     ap.add_argument("case", choices=["direct", "direct-aos", "direct-cutoff", "integrate", "update",
-                                     "compensated", "fp64", "bh"])
+                                     "compensated", "fp64", "bh", "bh-disk", "batched"])
     ap.add_argument("--n", type=int, default=1 << 18)
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--theta", type=float, default=0.5)
     a = ap.parse_args(argv)
 
     layout = native.LAYOUT_AOS if a.case == "direct-aos" else native.LAYOUT_SOA
+    if a.case == "batched":
+        # 512 Plummer systems, log-uniform sizes in [64, 8192]; one autotuned step per --steps
+        bodies, off = scenes.batch_plummer()
+        p = native.params(mode=native.MODE_BATCHED, law=native.LAW_SOFTENED, eps2=1e-4, dt=1e-3, size=0.0)
+        with native.Context() as ctx:
+            ctx.upload_bodies(bodies)
+            ctx.set_systems(off)
+            ctx.batch_set_config(15)
+            ctx.update(p, a.steps)
+            ctx.synchronize()
+            print(f"batched: bodies={len(bodies)} steps={a.steps} launches={ctx.launches()}")
+        return 0
+    if a.case == "bh-disk":
+        # the 16.8M disk + halo workload, scaled to --n bodies (same 12 : 4.777 split)
+        n_disk = int(round(a.n * 12_000_000 / 16_777_216))
+        bodies = scenes.disk_halo(n_disk=n_disk, n_halo=a.n - n_disk)
+        p = native.params(mode=native.MODE_NLOGN, theta=a.theta, law=native.LAW_SOFTENED, eps2=0.005 ** 2,
+                          dt=2.5e-4, size=0.0, tree_box=1, precision=native.PREC_COMPENSATED)
+        with native.Context() as ctx:
+            ctx.upload_bodies(bodies)
+            ctx.update(p, a.steps)
+            ctx.synchronize()
+            print(f"bh-disk: n={a.n} steps={a.steps} launches={ctx.launches()} stats={ctx.bh_stats()}")
+        return 0
     if a.case == "bh":
         bodies = scenes.two_plummer(a.n // 2)
     else:
