@@ -242,13 +242,10 @@ def _bench_gpu(args, stream):
         torch.distributed.barrier()
     ctx.synchronize()
     launches = ctx.launches() - launches0
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    # replicas only: the slowest rank's time, every rank's bodies
+    from nbody_gb300.replicas import whole_job_value
+    value, total_ms, _ = whole_job_value(sum(step_ms), N, args.steps, device="cuda")
     ms_per_step = total_ms / args.steps
-    value = N * args.steps * world / (total_ms * 1e-3)
 
     # --- the dominant kernel alone (accelerate), for the roofline ---
     acc_ms = statistics.mean(timed_steps(torch, stream, flush, lambda: ctx.accelerate(p), 3))

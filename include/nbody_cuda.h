@@ -304,6 +304,13 @@ int nbody_cuda_calibrate_fp32(nbody_cuda* ctx, double* tflops_scalar, double* tf
  * form's roofline. Synchronous. */
 int nbody_cuda_calibrate_fp64(nbody_cuda* ctx, double* tflops);
 
+/* Failure-path self-test: one kernel waits, with the same bounded wait every TMA pipeline
+ * uses, on an mbarrier phase that nothing completes, and gives up after limit_ns
+ * (at most 0.1 s). Returns NBODY_ERR_TIMEOUT -- the status a stuck copy would produce --
+ * and leaves the context usable. No reference counterpart (its fence waits are unbounded,
+ * source/gpu.cpp:780). Synchronous. */
+int nbody_cuda_selftest_wait(nbody_cuda* ctx, uint64_t limit_ns);
+
 #ifdef __cplusplus
 }
 #endif

@@ -144,3 +144,36 @@ extern "C" int nbody_cuda_calibrate_fp64(nbody_cuda* ctx, double* tflops)
     *tflops = static_cast<double>(blocks) * threads * iters * 8.0 * 2.0 / (best * 1e-3) / 1e12;
     return NBODY_OK;
 }
+
+namespace nbg
+{
+    // Waits on an mbarrier phase that nothing completes (one arrival expected, none made,
+    // no copy issued), with the bounded wait every pipeline uses, so the give-up path runs:
+    // the wait returns after limit_ns, sets DEV_ERR_TIMEOUT and the kernel exits normally.
+    __global__ void selftest_wait_kernel(unsigned* err, const unsigned long long limit_ns)
+    {
+        __shared__ __align__(8) uint64_t bar;
+        if (threadIdx.x == 0)
+        {
+            mbar_init(&bar, 1);
+            fence_mbar_init();
+        }
+        __syncthreads();
+        mbar_wait_bounded(&bar, 0, err, limit_ns);
+    }
+}
+
+extern "C" int nbody_cuda_selftest_wait(nbody_cuda* ctx, const uint64_t limit_ns)
+{
+    using namespace nbg;
+    if (!ctx)
+        return NBODY_ERR_INVALID;
+    if (limit_ns == 0 || limit_ns > 100000000ull)
+        return ctx_fail(ctx, NBODY_ERR_INVALID, "self-test wait limit must be in (0, 0.1 s]");
+    selftest_wait_kernel<<<1, 32, 0, ctx->stream>>>(ctx->dev_error, limit_ns);
+    ++ctx->launches;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return ctx_cuda_fail(ctx, e, "self-test launch");
+    return check_device_error(ctx);
+}

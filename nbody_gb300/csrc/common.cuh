@@ -62,10 +62,10 @@ namespace nbg
         return ok != 0;
     }
 
-    // Wait for phase `parity` of `bar` to complete, giving up after kWaitLimitNs.
+    // Wait for phase `parity` of `bar` to complete, giving up after limit_ns.
     // Returns false on timeout (and records it in *err).
     __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, const unsigned parity,
-                                                      unsigned* err)
+                                                      unsigned* err, const uint64_t limit_ns = kWaitLimitNs)
     {
         if (mbar_try_wait(bar, parity))
             return true;
@@ -74,7 +74,7 @@ namespace nbg
         {
             if (mbar_try_wait(bar, parity))
                 return true;
-            if (globaltimer() - start > kWaitLimitNs)
+            if (globaltimer() - start > limit_ns)
             {
                 atomicOr(err, DEV_ERR_TIMEOUT);
                 return false;

@@ -40,6 +40,7 @@ EXPORTS = (
     "nbody_cuda_batch_config_count", "nbody_cuda_batch_config", "nbody_cuda_batch_set_config",
     "nbody_cuda_system_energy", "nbody_cuda_update_graph", "nbody_cuda_direct_variant_count",
     "nbody_cuda_direct_variant", "nbody_cuda_set_direct_variant", "nbody_cuda_direct_autotune",
+    "nbody_cuda_selftest_wait",
 )
 
 
@@ -116,6 +117,7 @@ def lib() -> C.CDLL:
         "nbody_cuda_direct_variant": ([C.c_int] + [C.POINTER(C.c_int)] * 3, C.c_int),
         "nbody_cuda_set_direct_variant": ([vp, C.c_int], C.c_int),
         "nbody_cuda_direct_autotune": ([vp, P, vp, sz, C.POINTER(C.c_int)], C.c_int),
+        "nbody_cuda_selftest_wait": ([vp, C.c_uint64], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

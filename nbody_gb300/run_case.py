@@ -24,6 +24,7 @@ def main(argv=None) -> int:
     ap.add_argument("--n", type=int, default=1 << 18)
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--variant", type=int, default=-1, help="pin a direct-sum kernel shape")
     a = ap.parse_args(argv)
 
     layout = native.LAYOUT_AOS if a.case == "direct-aos" else native.LAYOUT_SOA
@@ -62,6 +63,8 @@ def main(argv=None) -> int:
                       size=64.0)
     with native.Context(layout) as ctx:
         ctx.upload_bodies(bodies)
+        if a.variant >= 0:
+            ctx.set_direct_variant(a.variant)
         for _ in range(a.steps):
             if a.case == "integrate":
                 ctx.integrate(p)
