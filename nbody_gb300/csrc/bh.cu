@@ -419,17 +419,17 @@ namespace nbg
     }
 
     template <int LAW>
-    __global__ void __launch_bounds__(kTravWarps * 32) traverse_kernel(
+    __global__ void __launch_bounds__(kTravWarps * 32, 4) traverse_kernel(
         const OctNode* __restrict__ nodes, const float4* __restrict__ spm, const float* __restrict__ srad,
         const uint32_t* __restrict__ order, const int n, const float G, const float eps2,
         float4* __restrict__ acc, float* __restrict__ body_out, unsigned* __restrict__ err,
         unsigned long long* __restrict__ stats)
     {
-        __shared__ int stk_node[kTravWarps][kStack];
-        __shared__ unsigned stk_mask[kTravWarps][kStack];
+        // one 8-byte entry per stacked cell: {cell index, mask of the lanes that opened it}
+        __shared__ int2 stk[kTravWarps][kStack];
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         const unsigned lt = (1u << lane) - 1u;
-        unsigned long long inter = 0, visits = 0;
+        unsigned inter = 0, visits = 0;
 
         for (int tile = blockIdx.x * kTravWarps + warp; tile * 32 < n; tile += gridDim.x * kTravWarps)
         {
@@ -441,37 +441,41 @@ namespace nbg
             float ax = 0.f, ay = 0.f, az = 0.f;
             const unsigned valid_mask = __ballot_sync(0xffffffffu, valid);
             if (lane == 0)
-            {
-                stk_node[warp][0] = 0;
-                stk_mask[warp][0] = valid_mask;
-            }
+                stk[warp][0] = make_int2(0, static_cast<int>(valid_mask));
             int sp = 1;
             __syncwarp();
             // Each cell is reached from its one parent, so a warp pops at most one entry
             // per cell (< n). The bound only trips on a malformed tree: it records the
             // error and stops this warp instead of spinning.
-            long long guard = 0;
+            int guard = 0;
+            const int guard_limit = n + 64;
             while (sp > 0)
             {
-                if (++guard > static_cast<long long>(n) + 64)
+                if (++guard > guard_limit)
                 {
                     if (lane == 0)
                         atomicOr(err, DEV_ERR_BOUNDS);
                     break;
                 }
                 --sp;
-                const int nd = stk_node[warp][sp];
-                const unsigned mask = stk_mask[warp][sp];
+                const int2 top = stk[warp][sp];
                 __syncwarp();
+                const int nd = top.x;
+                const unsigned mask = static_cast<unsigned>(top.y);
                 ++visits;
-                const float4 cm = nodes[nd].com_mass;
+                const OctNode* cell = nodes + nd;
+                // the three loads of a visit issue together: centre of mass + mass;
+                // open_r2, nchild, first, last; this lane's child slot
+                const float4 cm = cell->com_mass;
+                const int4 meta = *reinterpret_cast<const int4*>(&cell->open_r2);
+                const int cslot = cell->child[lane & 7];
                 if (cm.w == 0.f)
                     continue;       // bhtree.cpp:109-113: empty nodes are skipped
                 const bool in = (mask >> lane) & 1u;
                 // bhtree.cpp:117-125, evaluated in the reference's operation order
                 const float dx = __fsub_rn(cm.x, me.x), dy = __fsub_rn(cm.y, me.y), dz = __fsub_rn(cm.z, me.z);
                 const float dist_sq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                const bool accept = in && dist_sq > nodes[nd].open_r2;
+                const bool accept = in && dist_sq > __int_as_float(meta.x);
                 if (accept)
                 {
                     apply<LAW>(me.x, me.y, me.z, lim, cm.x, cm.y, cm.z, cm.w, ax, ay, az);
@@ -481,11 +485,10 @@ namespace nbg
                 if (!open)
                     continue;
                 const bool mine = (open >> lane) & 1u;
-                const int nchild = nodes[nd].nchild;
+                const int nchild = meta.y;
                 if (nchild < 0)
                 {
-                    const int first = nodes[nd].first, last = nodes[nd].last;
-                    for (int b = first; b <= last; ++b)
+                    for (int b = meta.z; b <= meta.w; ++b)
                     {
                         const float4 s = spm[b];
                         if (mine)
@@ -496,19 +499,19 @@ namespace nbg
                     }
                     continue;
                 }
-                const int c = lane < nchild ? nodes[nd].child[lane] : 0;
+                const int c = lane < nchild ? cslot : 0;
                 const bool is_cell = lane < nchild && c >= 0;
                 const bool is_leaf = lane < nchild && c < 0;
+                // each child lane fetches its own leaf body, so the leaf loop below only
+                // broadcasts registers
+                const float4 leaf = is_leaf ? spm[~c] : make_float4(0.f, 0.f, 0.f, 0.f);
                 const unsigned cells = __ballot_sync(0xffffffffu, is_cell);
-                unsigned leaves = __ballot_sync(0xffffffffu, is_leaf);
+                unsigned leaves = __ballot_sync(0xffffffffu, is_leaf && leaf.w != 0.f);
                 if (is_cell)
                 {
                     const int at = sp + __popc(cells & lt);
                     if (at < kStack)
-                    {
-                        stk_node[warp][at] = c;
-                        stk_mask[warp][at] = open;
-                    }
+                        stk[warp][at] = make_int2(c, static_cast<int>(open));
                     else
                         atomicOr(err, DEV_ERR_BOUNDS);
                 }
@@ -518,11 +521,13 @@ namespace nbg
                 {
                     const int l = __ffs(leaves) - 1;
                     leaves &= leaves - 1;
-                    const int b = ~__shfl_sync(0xffffffffu, c, l);
-                    const float4 s = spm[b];
-                    if (mine && s.w != 0.f)
+                    const float sx = __shfl_sync(0xffffffffu, leaf.x, l);
+                    const float sy = __shfl_sync(0xffffffffu, leaf.y, l);
+                    const float sz = __shfl_sync(0xffffffffu, leaf.z, l);
+                    const float sw = __shfl_sync(0xffffffffu, leaf.w, l);
+                    if (mine)
                     {
-                        apply<LAW>(me.x, me.y, me.z, lim, s.x, s.y, s.z, s.w, ax, ay, az);
+                        apply<LAW>(me.x, me.y, me.z, lim, sx, sy, sz, sw, ax, ay, az);
                         ++inter;
                     }
                 }
@@ -542,12 +547,13 @@ namespace nbg
             }
         }
         // per-warp totals
+        unsigned long long total = inter;
         for (int o = 16; o > 0; o >>= 1)
-            inter += __shfl_down_sync(0xffffffffu, inter, o);
+            total += __shfl_down_sync(0xffffffffu, total, o);
         if (lane == 0)
         {
-            atomicAdd(&stats[0], inter);
-            atomicAdd(&stats[1], visits);
+            atomicAdd(&stats[0], total);
+            atomicAdd(&stats[1], static_cast<unsigned long long>(visits));
         }
     }
 
