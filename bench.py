@@ -399,9 +399,9 @@ def bench_bh16m(torch, stream, flush, native, scenes, args):
             ctx.accelerate(p)
             stats = ctx.bh_stats()
             ms_step = sum(ms) / steps
-            # compulsory bytes per step (byte model): bbox 16, Morton 16+8, sort 8 passes x 24,
-            # permute 32, build ~56 per internal node, COM ~48 per node, integrate 80 (+32 comp)
-            build_b = n * (16 + 24 + 8 * 24 + 32 + 56 + 48) + n * (80 + 48)
+            # compulsory bytes per step (byte model): bbox 16, Morton 16+8, sort 7 passes x 24,
+            # permute 32, build ~56 per internal node, COM ~48 per node, integrate 80 (+48 comp)
+            build_b = n * (16 + 24 + 7 * 24 + 32 + 56 + 48) + n * (80 + 48)
             trav_b = 16 * stats["interactions"] + 64 * stats["visits"]
             res[f"theta_{theta}"] = {
                 "steps_per_s": 1e3 / ms_step, "ms_per_step": ms_step, "body_steps_per_s": n * 1e3 / ms_step,
@@ -414,7 +414,74 @@ def bench_bh16m(torch, stream, flush, native, scenes, args):
                              "bytes_model": "build+integrate ~%d B/body, traversal 16 B/interaction + 64 B/cell "
                                             "visit (mostly L2 hits)" % ((build_b) // n)},
             }
+        p = native.params(mode=native.MODE_NLOGN, theta=0.5, law=native.LAW_SOFTENED, eps2=0.005 ** 2,
+                          dt=2.5e-4, size=0.0, tree_box=1, precision=native.PREC_COMPENSATED)
+        res["transfer"] = bench_transfer(torch, native, ctx, b, p)
     return res
+
+
+def bench_transfer(torch, native, ctx, bodies, p, reps=3):
+    """Host transfers of all N Body records (48 B each) on each path, against the copy
+    engine's own pinned-memory bandwidth for the same bytes (the link roofline), and one
+    frame of the reference's read-every-frame loop: update(dt) then state()."""
+    n = len(bodies)
+    nbytes = n * 48
+    host = np.empty_like(bodies)
+
+    def best(fn):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    dev = torch.empty(nbytes // 4, dtype=torch.float32, device="cuda")
+    pin = torch.empty(nbytes // 4, dtype=torch.float32, pin_memory=True)
+    ce_d2h = nbytes / best(lambda: (pin.copy_(dev, non_blocking=True), torch.cuda.synchronize())) / 1e9
+    ce_h2d = nbytes / best(lambda: (dev.copy_(pin, non_blocking=True), torch.cuda.synchronize())) / 1e9
+    del dev, pin
+    info = ctx.transfer_info()
+    out = {"n_bodies": n, "bytes": nbytes, "pageable_access": info["pageable"],
+           "auto_resolves_to": {1: "staged", 2: "mapped", 3: "direct"}[info["resolved"]],
+           "copy_engine_gbs": {"d2h_pinned": ce_d2h, "h2d_pinned": ce_h2d},
+           "caller_memory": "pageable numpy array", "timing": "host wall clock, best of %d" % reps}
+    names = {native.TRANSFER_STAGED: "staged", native.TRANSFER_MAPPED: "mapped", native.TRANSFER_DIRECT: "direct"}
+    ctx.upload_bodies(bodies)
+    for pol, name in names.items():
+        try:
+            ctx.set_transfer(pol)
+        except native.NbodyError as e:
+            out[name] = {"unavailable": str(e)}
+            continue
+        up = best(lambda: ctx.upload_bodies(bodies))
+        down = best(lambda: ctx.download_bodies(into=host))
+        pos = best(lambda: ctx.download_bodies(mask=native.READ_POSITIONS, into=host))
+        out[name] = {"upload_ms": up * 1e3, "upload_gbs": nbytes / up / 1e9,
+                     "download_ms": down * 1e3, "download_gbs": nbytes / down / 1e9,
+                     "download_positions_ms": pos * 1e3,
+                     "roofline": {"bound": "host link", "unit": "GB/s", "peak_source": "copy engine, same bytes",
+                                  "download_frac": nbytes / down / 1e9 / ce_d2h,
+                                  "upload_frac": nbytes / up / 1e9 / ce_h2d}}
+    ctx.upload_bodies(bodies)
+    frames = {}
+    for pol, name in names.items():
+        try:
+            ctx.set_transfer(pol)
+        except native.NbodyError:
+            continue
+        def frame():
+            ctx.update(p, 1)
+            ctx.prefetch(native.READ_ALL)       # the prediction of a read-every-frame caller
+            ctx.download_bodies(into=host)
+        frames[name] = best(frame) * 1e3
+    ctx.set_transfer(native.TRANSFER_AUTO)
+    frames["step_only"] = best(lambda: (ctx.update(p, 1), ctx.synchronize())) * 1e3
+    out["frame_ms"] = frames
+    out["frame_note"] = ("BH theta=0.5 step (compensated integration) + full Body readback into the caller's "
+                         "array, per path; step_only is the same step without the readback")
+    return out
 
 
 def fp64_euler_drift(bodies, eps2, dt, steps):

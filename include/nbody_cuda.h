@@ -157,6 +157,44 @@ int nbody_cuda_upload_soa(nbody_cuda* ctx, const float* pos_mass, const float* v
 int nbody_cuda_download_soa(nbody_cuda* ctx, float* pos_mass, float* vel_radius, float* acc,
                             size_t n);
 
+/* --- host transfer policy -------------------------------------------------------------- */
+
+/* How nbody_cuda_upload_bodies / download_bodies move Body records between the caller's
+ * host array and the device streams. The reference always goes through mapped staging
+ * allocations and a host-side (de)interleave (gpu_solver_split.h:155-177, 188-221). */
+typedef enum nbody_transfer
+{
+    NBODY_TRANSFER_AUTO = 0,    /* DIRECT where the device reaches pageable host memory
+                                   through the host's page tables (a coherent host link,
+                                   as NVLink-C2C), else MAPPED */
+    NBODY_TRANSFER_STAGED = 1,  /* (de)interleave on the device, copy engine to/from pinned
+                                   staging, host copy to/from the caller's array */
+    NBODY_TRANSFER_MAPPED = 2,  /* a kernel writes/reads the records in page-locked mapped
+                                   staging directly (zero-copy), host copy to/from the caller */
+    NBODY_TRANSFER_DIRECT = 3   /* a kernel writes/reads the caller's own array: no staging
+                                   and no host copy. Needs pageable memory access */
+} nbody_transfer;
+
+/* Select the transfer path. DIRECT on a device without pageable memory access returns
+ * NBODY_ERR_UNSUPPORTED and leaves the policy unchanged. No reference counterpart. */
+int nbody_cuda_set_transfer(nbody_cuda* ctx, int policy);
+
+/* The policy selected, the path AUTO resolves to, whether the device accesses pageable
+ * host memory (0/1; 2 = through the host's page tables), and how many downloads were
+ * served from a predicted readback. Any pointer may be NULL. */
+int nbody_cuda_transfer_info(const nbody_cuda* ctx, int* policy, int* resolved, int* pageable,
+                             uint64_t* readback_hits);
+
+/* Predicted readback: queue, behind the work already on the stream, a copy of the
+ * streams in `mask` into the context's mapped staging, so that a later
+ * nbody_cuda_download_bodies asking for no more than `mask` only waits for that copy and
+ * takes the records from host memory. Valid until a call changes the device bodies. When
+ * the resolved path is DIRECT the call queues nothing: a download then writes the
+ * caller's array straight from the device, which moves the same bytes once. Replaces the
+ * Readback argument of GpuDevice::step (source/gpu.cpp:842-875) chosen by
+ * GpuSolverSplit::wanted_readback (gpu_solver_split.h:122-132). */
+int nbody_cuda_prefetch(nbody_cuda* ctx, unsigned mask);
+
 /* --- stepping (queued, asynchronous) --------------------------------------------------- */
 
 /* Accelerations for every body. Replaces GpuDevice::accelerate (source/gpu.cpp:799-841). */

@@ -68,17 +68,6 @@ namespace
         return f && std::strcmp(f, what) == 0;
     }
 
-    bool is_pinned(const void* p)
-    {
-        cudaPointerAttributes a{};
-        if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
-        {
-            cudaGetLastError();
-            return false;
-        }
-        return a.type == cudaMemoryTypeHost;
-    }
-
     int check_params(nbody_cuda* ctx, const nbody_step_params* p)
     {
         if (!p)
@@ -100,6 +89,17 @@ namespace
 // ---------------------------------------------------------------------------------------
 namespace nbg
 {
+    bool is_pinned(const void* p)
+    {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return false;
+        }
+        return a.type == cudaMemoryTypeHost;
+    }
+
     int ctx_fail(nbody_cuda* ctx, const int status, const char* msg)
     {
         return fail(ctx, status, "%s", msg);
@@ -226,6 +226,19 @@ int nbody_cuda_create(nbody_cuda** out, const int layout)
         return s;
     }
     ctx->stream = ctx->own_stream;
+    cudaDeviceGetAttribute(&ctx->pageable_access, cudaDevAttrPageableMemoryAccess, ctx->device);
+    cudaDeviceGetAttribute(&ctx->pageable_host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, ctx->device);
+    cudaGetLastError();
+    // NBODY_CUDA_TRANSFER=staged|mapped|direct picks the initial transfer path (default auto),
+    // so that a whole program can be run over each path unchanged.
+    if (const char* t = std::getenv("NBODY_CUDA_TRANSFER"))
+    {
+        const int policy = !std::strcmp(t, "staged") ? NBODY_TRANSFER_STAGED
+                           : !std::strcmp(t, "mapped") ? NBODY_TRANSFER_MAPPED
+                           : (!std::strcmp(t, "direct") && ctx->pageable_access) ? NBODY_TRANSFER_DIRECT
+                                                                                 : NBODY_TRANSFER_AUTO;
+        ctx->transfer = policy;
+    }
     *out = ctx;
     return NBODY_OK;
 }
@@ -239,6 +252,7 @@ void nbody_cuda_destroy(nbody_cuda* ctx)
     release_bh(ctx);
     release_precise(ctx);
     release_batch(ctx);
+    release_transfer(ctx);
     if (ctx->graph)
         cudaGraphExecDestroy(ctx->graph);
     cudaFree(ctx->pm);
@@ -343,7 +357,9 @@ int nbody_cuda_reserve(nbody_cuda* ctx, const size_t n)
     return NBODY_OK;
 }
 
-namespace
+}   // extern "C"
+
+namespace nbg
 {
     // Pinned staging, reused across calls; waits for the previous transfer through it.
     int staging(nbody_cuda* ctx, const size_t bytes, void** out)
@@ -380,7 +396,7 @@ namespace
         void* stage = nullptr;
         if (const int st = staging(ctx, bytes, &stage))
             return st;
-        std::memcpy(stage, src, bytes);
+        host_copy(stage, src, bytes);
         NBG_CUDA(ctx, cudaMemcpyAsync(dst, stage, bytes, cudaMemcpyHostToDevice, ctx->stream), "host to device copy");
         NBG_CUDA(ctx, cudaEventRecord(ctx->pinned_event, ctx->stream), "event record");
         return NBODY_OK;
@@ -402,7 +418,7 @@ namespace
         NBG_CUDA(ctx, cudaMemcpyAsync(stage, src, bytes, cudaMemcpyDeviceToHost, ctx->stream), "device to host copy");
         if (const int st = check_device_error(ctx))
             return st;
-        std::memcpy(dst, stage, bytes);
+        host_copy(dst, stage, bytes);
         return NBODY_OK;
     }
 
@@ -421,6 +437,8 @@ namespace
     }
 }
 
+extern "C" {
+
 int nbody_cuda_upload_bodies(nbody_cuda* ctx, const void* bodies, const size_t n)
 {
     if (!ctx || (!bodies && n))
@@ -431,17 +449,10 @@ int nbody_cuda_upload_bodies(nbody_cuda* ctx, const void* bodies, const size_t n
         ++ctx->generation;      // the body count is an argument of captured launches
     ctx->count = n;
     ctx->origin_valid = false;
+    ++ctx->body_version;
     if (!n)
         return NBODY_OK;
-    if (ctx->layout == NBODY_LAYOUT_AOS)
-        return h2d(ctx, ctx->bodies, bodies, n * 48);
-    if (const int st = ensure_aos_stage(ctx, n))
-        return st;
-    if (const int st = h2d(ctx, ctx->aos_stage, bodies, n * 48))
-        return st;
-    NBG_CUDA(ctx, launch_split(ctx->aos_stage, ctx->pm, ctx->vr, ctx->acc, static_cast<int>(n), ctx->stream, &ctx->launches),
-             "split launch");
-    return NBODY_OK;
+    return upload_records(ctx, bodies, n);
 }
 
 int nbody_cuda_download_bodies(nbody_cuda* ctx, void* bodies, const size_t n, const unsigned mask)
@@ -453,44 +464,7 @@ int nbody_cuda_download_bodies(nbody_cuda* ctx, void* bodies, const size_t n, co
         return check_device_error(ctx);
     if (const int st = sync_precise_positions(ctx))
         return st;
-    const float* dev = ctx->bodies;
-    if (ctx->layout == NBODY_LAYOUT_SOA)
-    {
-        if (const int st = ensure_aos_stage(ctx, take))
-            return st;
-        NBG_CUDA(ctx, launch_join(ctx->pm, ctx->vr, ctx->acc, ctx->aos_stage, static_cast<int>(take), ctx->stream, &ctx->launches),
-                 "join launch");
-        dev = ctx->aos_stage;
-    }
-    if ((mask & NBODY_READ_ALL) == NBODY_READ_ALL)
-        return d2h(ctx, bodies, dev, take * 48);
-    // Merge only the selected fields into the caller's records.
-    void* stage = nullptr;
-    if (const int st = staging(ctx, take * 48, &stage))
-        return st;
-    NBG_CUDA(ctx, cudaMemcpyAsync(stage, dev, take * 48, cudaMemcpyDeviceToHost, ctx->stream), "device to host copy");
-    if (const int st = check_device_error(ctx))
-        return st;
-    const float* s = static_cast<const float*>(stage);
-    float* d = static_cast<float*>(bodies);
-    for (size_t i = 0; i < take; ++i)
-    {
-        const float* si = s + 12 * i;
-        float* di = d + 12 * i;
-        if (mask & NBODY_READ_POSITIONS)
-        {
-            di[0] = si[0]; di[1] = si[1]; di[2] = si[2]; di[7] = si[7];
-        }
-        if (mask & NBODY_READ_VELOCITIES)
-        {
-            di[4] = si[4]; di[5] = si[5]; di[6] = si[6]; di[3] = si[3];
-        }
-        if (mask & NBODY_READ_ACCELERATIONS)
-        {
-            di[8] = si[8]; di[9] = si[9]; di[10] = si[10];
-        }
-    }
-    return NBODY_OK;
+    return download_records(ctx, bodies, take, mask & NBODY_READ_ALL);
 }
 
 int nbody_cuda_upload_soa(nbody_cuda* ctx, const float* pos_mass, const float* vel_radius, const float* acc,
@@ -506,6 +480,7 @@ int nbody_cuda_upload_soa(nbody_cuda* ctx, const float* pos_mass, const float* v
         ++ctx->generation;      // the body count is an argument of captured launches
     ctx->count = n;
     ctx->origin_valid = false;
+    ++ctx->body_version;
     int st = NBODY_OK;
     if (pos_mass && (st = h2d(ctx, ctx->pm, pos_mass, n * 16)))
         return st;
@@ -621,6 +596,7 @@ int nbody_cuda_accelerate(nbody_cuda* ctx, const nbody_step_params* p)
         return st;
     if (!ctx->count)
         return NBODY_OK;
+    ++ctx->body_version;
     return accelerate_impl(ctx, p, false);
 }
 
@@ -633,6 +609,7 @@ int nbody_cuda_integrate(nbody_cuda* ctx, const nbody_step_params* p)
     if (!ctx->count)
         return NBODY_OK;
     ctx->pending_partials = 0;
+    ++ctx->body_version;
     return integrate_impl(ctx, p);
 }
 
@@ -646,6 +623,7 @@ int nbody_cuda_update(nbody_cuda* ctx, const nbody_step_params* p, const int ste
         return fail(ctx, NBODY_ERR_INVALID, "negative step count");
     if (!ctx->count)
         return NBODY_OK;
+    ++ctx->body_version;
     for (int s = 0; s < steps; ++s)
     {
         if (const int st = accelerate_impl(ctx, p, true))
@@ -833,6 +811,7 @@ int nbody_cuda_update_graph(nbody_cuda* ctx, const nbody_step_params* p, const i
         return fail(ctx, NBODY_ERR_INVALID, "negative step count");
     if (!ctx->count || steps == 0)
         return NBODY_OK;
+    ++ctx->body_version;
     // The first step runs eagerly: it grows every buffer the step needs, so nothing
     // allocates while the step is captured.
     if (const int st = nbody_cuda_update(ctx, p, 1))

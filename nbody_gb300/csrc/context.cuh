@@ -47,6 +47,23 @@ struct nbody_cuda
     size_t pinned_bytes = 0;
     cudaEvent_t pinned_event = nullptr;
 
+    // Transfer paths (transfer.cu). `mapped` is page-locked host memory the kernels write
+    // and read directly over the host link; it also holds the predicted readback, which is
+    // current while `body_version` has not moved since it was enqueued.
+    int transfer = NBODY_TRANSFER_AUTO;
+    int pageable_access = 0;        // cudaDevAttrPageableMemoryAccess
+    int pageable_host_tables = 0;   // cudaDevAttrPageableMemoryAccessUsesHostPageTables
+    void* mapped = nullptr;
+    void* mapped_dev = nullptr;
+    size_t mapped_bytes = 0;
+    cudaEvent_t mapped_event = nullptr;   // the last device access to `mapped`
+    uint64_t body_version = 0;      // bumped by every call that may change the device bodies
+    bool readback_valid = false;
+    uint64_t readback_version = 0;
+    size_t readback_count = 0;
+    unsigned readback_mask = 0;
+    uint64_t readback_hits = 0;
+
     unsigned* dev_error = nullptr;  // device error word (nbg::DEV_ERR_*)
 
     // Split-precision state (direct_precise.cu): FP64 origin + FP32 offsets live on the
@@ -90,6 +107,20 @@ namespace nbg
     // pointers a graph holds must stay valid), and it retires any captured graph.
     int before_allocation(nbody_cuda* ctx);
     int check_device_error(nbody_cuda* ctx);
+
+    // context.cu: copies through the pinned staging buffer, and the device-side Body staging
+    int staging(nbody_cuda* ctx, size_t bytes, void** out);
+    int h2d(nbody_cuda* ctx, void* dst, const void* src, size_t bytes);
+    int d2h(nbody_cuda* ctx, void* dst, const void* src, size_t bytes);
+    int ensure_aos_stage(nbody_cuda* ctx, size_t n);
+    bool is_pinned(const void* p);
+
+    // transfer.cu
+    void host_copy(void* dst, const void* src, size_t bytes);     // split across threads when large
+    int download_records(nbody_cuda* ctx, void* bodies, size_t take, unsigned mask);
+    int upload_records(nbody_cuda* ctx, const void* bodies, size_t n);
+    int prefetch_records(nbody_cuda* ctx, unsigned mask);
+    void release_transfer(nbody_cuda* ctx);
 
     // direct_precise.cu
     int precise_accelerate(nbody_cuda* ctx, const nbody_step_params* p);

@@ -9,7 +9,12 @@
 //   - steps leave their results on the device; state() materialises them into
 //     State::bodies, reading only min(bodies.size(), device count) (gpu_solver_split.h:202);
 //   - an empty body array launches nothing (gpu_solver_split.h:56-59);
-//   - G, theta, size and wrap are read from the State at every step.
+//   - G, theta, size and wrap are read from the State at every step;
+//   - update() predicts the next read as the reference does (wanted_readback,
+//     gpu_solver_split.h:122-132): when a state() followed the previous step, the step
+//     queues the readback behind itself (nbody_cuda_prefetch), and state() then only waits
+//     for it. Where the library resolves the transfer to DIRECT (a coherent host link), the
+//     prefetch queues nothing and state() has the device write State::bodies directly.
 // Unlike the reference, the Barnes-Hut tree is built on the device; tree() exports it into
 // the reference's node layout on demand.
 //
@@ -95,6 +100,8 @@ namespace nbody
             const nbody_step_params p = params(dt);
             check(nbody_cuda_update(_dev, &p, 1), "update");
             stepped();
+            if (const unsigned want = wanted_readback())
+                check(nbody_cuda_prefetch(_dev, want), "readback");
         }
 
         [[nodiscard]] const bh::Tree* tree() const override
@@ -188,8 +195,18 @@ namespace nbody
             }
         }
 
+        // Everything, if the last step was followed by a read: a caller that reads every
+        // frame will read again. The device tree needs no positions on the host.
+        [[nodiscard]] unsigned wanted_readback() const
+        {
+            const unsigned want = _materialize_expected ? NBODY_READ_ALL : 0u;
+            _materialize_expected = false;
+            return want;
+        }
+
         void materialize() const
         {
+            _materialize_expected = true;   // set even when there is nothing to fetch
             if (!_device_dirty || _host_dirty)
                 return;
             const size_t n = _state->bodies.size();
@@ -201,6 +218,7 @@ namespace nbody
         CudaSolverConfig _config;
         mutable bool _host_dirty = true;
         mutable bool _device_dirty = false;
+        mutable bool _materialize_expected = false;
         mutable bh::Tree _tree;
         mutable bool _tree_valid = false;
         uint64_t _tree_build = 0;

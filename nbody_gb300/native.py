@@ -20,6 +20,7 @@ LAW_CUTOFF, LAW_SOFTENED = 0, 1
 PREC_FP32, PREC_COMPENSATED, PREC_FP64 = 0, 1, 2
 LAYOUT_SOA, LAYOUT_AOS = 0, 1
 READ_POSITIONS, READ_VELOCITIES, READ_ACCELERATIONS, READ_ALL = 1, 2, 4, 7
+TRANSFER_AUTO, TRANSFER_STAGED, TRANSFER_MAPPED, TRANSFER_DIRECT = 0, 1, 2, 3
 
 # bh::Node (include/nbody/bhtree.h of the reference): bounds centre, size, com, mass, links
 NODE_DTYPE = np.dtype([("center", "<f4", 3), ("size", "<f4"), ("com", "<f4", 3), ("mass", "<f4"),
@@ -40,7 +41,8 @@ EXPORTS = (
     "nbody_cuda_batch_config_count", "nbody_cuda_batch_config", "nbody_cuda_batch_set_config",
     "nbody_cuda_system_energy", "nbody_cuda_update_graph", "nbody_cuda_direct_variant_count",
     "nbody_cuda_direct_variant", "nbody_cuda_set_direct_variant", "nbody_cuda_direct_autotune",
-    "nbody_cuda_selftest_wait",
+    "nbody_cuda_selftest_wait", "nbody_cuda_set_transfer", "nbody_cuda_transfer_info",
+    "nbody_cuda_prefetch",
 )
 
 
@@ -118,6 +120,9 @@ def lib() -> C.CDLL:
         "nbody_cuda_set_direct_variant": ([vp, C.c_int], C.c_int),
         "nbody_cuda_direct_autotune": ([vp, P, vp, sz, C.POINTER(C.c_int)], C.c_int),
         "nbody_cuda_selftest_wait": ([vp, C.c_uint64], C.c_int),
+        "nbody_cuda_set_transfer": ([vp, C.c_int], C.c_int),
+        "nbody_cuda_transfer_info": ([vp] + [C.POINTER(C.c_int)] * 3 + [C.POINTER(C.c_uint64)], C.c_int),
+        "nbody_cuda_prefetch": ([vp, u], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -198,6 +203,19 @@ class Context:
 
     def count(self) -> int:
         return int(lib().nbody_cuda_count(self.h))
+
+    # --- transfer policy ---------------------------------------------------------
+    def set_transfer(self, policy: int):
+        self.check(lib().nbody_cuda_set_transfer(self.h, policy))
+
+    def transfer_info(self) -> dict:
+        pol, res, pg = C.c_int(), C.c_int(), C.c_int()
+        hits = C.c_uint64()
+        self.check(lib().nbody_cuda_transfer_info(self.h, C.byref(pol), C.byref(res), C.byref(pg), C.byref(hits)))
+        return {"policy": pol.value, "resolved": res.value, "pageable": pg.value, "readback_hits": hits.value}
+
+    def prefetch(self, mask: int = READ_ALL):
+        self.check(lib().nbody_cuda_prefetch(self.h, mask))
 
     def reserve(self, n: int):
         self.check(lib().nbody_cuda_reserve(self.h, n))

@@ -60,8 +60,12 @@ def solver_test_binary(cuda_lib, tmp_path_factory):
 
 
 @pytest.mark.gpu
-def test_cuda_solver_suite(solver_test_binary):
-    r = subprocess.run([str(solver_test_binary)], capture_output=True, text=True, timeout=600)
+@pytest.mark.parametrize("transfer", ["auto", "staged", "mapped"])
+def test_cuda_solver_suite(solver_test_binary, transfer):
+    """The whole suite once per host transfer path: the state the reference's read path
+    sees must not depend on how the bytes travel, nor on the predicted readback."""
+    env = dict(os.environ, NBODY_CUDA_TRANSFER=transfer)
+    r = subprocess.run([str(solver_test_binary)], capture_output=True, text=True, timeout=600, env=env)
     print(r.stdout)
     assert r.returncode == 0, r.stdout[-4000:] + r.stderr[-2000:]
     assert "FAIL" not in r.stdout
