@@ -23,7 +23,12 @@ Printed JSON line (rank 0):
                   dt = 2.5e-4, FP32 tree forces + compensated integration, reference-
                   convention theta 0.5 and 0.75: steps/s, interactions, tree cells, and the
                   per-stage byte model against the measured HBM copy bandwidth.
+                  Its "transfer" object times the host transfer paths (staged, mapped,
+                  direct) for all 16.8M Body records against the copy engine's pinned
+                  bandwidth, and one frame of update + state().
   configs         configs 1 (N = 4096 Plummer, 100 steps) and 2 (2 x 131072 Plummer BH).
+  scene_generators util::disk and util::cube on the device at N = 16,777,216, against the
+                  reference's serial generator on 1,048,576 bodies.
   cpu_baseline    the reference's CPU brute force (oracle/_ref, built from the reference's
                   sources) where it loads, else the oracle's C restatement, on all host
                   cores, timed on a bounded sample of targets against all N sources.
@@ -275,6 +280,7 @@ def _bench_gpu(args, stream):
         extra["configs"] = bench_small_configs(torch, stream, flush, native, scenes)
         extra["configs"]["config4_batched"] = bench_batched(torch, stream, flush, native, scenes,
                                                             float(N) * N / (acc_ms * 1e-3))
+        extra["scene_generators"] = bench_scenes(torch, stream, native)
 
     line = None
     if rank == 0:
@@ -481,6 +487,49 @@ def bench_transfer(torch, native, ctx, bodies, p, reps=3):
     out["frame_ms"] = frames
     out["frame_note"] = ("BH theta=0.5 step (compensated integration) + full Body readback into the caller's "
                          "array, per path; step_only is the same step without the readback")
+    return out
+
+
+def bench_scenes(torch, stream, native, reps=5):
+    """util::disk and util::cube generated on the device at N = 16,777,216, against the
+    reference's serial generator (oracle/_ref where it loads, else the oracle's bit-exact
+    restatement) on a bounded sample of 1,048,576 bodies."""
+    from oracle import oracle as O
+    n = 1 << 24
+    hbm = measured_peaks().get("hbm_gbs", 6800.0)
+    out = {"n_bodies": n, "args": "the reference's defaults (disk: outer radius 250, central mass 4.1e6; cube: edge 500)"}
+    with native.Context() as ctx:
+        ctx.set_stream(stream.cuda_stream)
+        for kind in ("disk", "cube"):
+            gen = getattr(ctx, f"scene_{kind}")
+            gen(n)
+            torch.cuda.synchronize()
+            ms = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                gen(n)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            best = min(ms)
+            out[kind] = {"device_ms": best, "bodies_per_s": n / (best * 1e-3),
+                         "roofline": {"bound": "issue (integer mulmod jump-ahead, FP64 sin/cos/log)",
+                                      "achieved": n * 48 / (best * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                                      "frac": n * 48 / (best * 1e-3) / 1e9 / hbm,
+                                      "note": "48 B written per body against the measured HBM copy bandwidth"}}
+    sample = 1 << 20
+    ref = O.ref_lib() is not None
+    t0 = time.perf_counter()
+    if ref:
+        O.ref_disk_range(np.zeros((sample, 12), np.float32), 0, sample)
+    else:
+        O.disk(sample)
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": sample / cpu_s, "unit": "bodies/s", "cores": 1,
+                           "kind": "reference" if ref else "port",
+                           "sample": "util::disk, 1,048,576 bodies (the reference's generator is serial)"}
+    out["disk_speedup_vs_cpu"] = out["disk"]["bodies_per_s"] / out["cpu_baseline"]["value"]
     return out
 
 

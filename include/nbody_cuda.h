@@ -195,6 +195,46 @@ int nbody_cuda_transfer_info(const nbody_cuda* ctx, int* policy, int* resolved, 
  * GpuSolverSplit::wanted_readback (gpu_solver_split.h:122-132). */
 int nbody_cuda_prefetch(nbody_cuda* ctx, unsigned mask);
 
+/* --- scene generators (queued) ---------------------------------------------------------- */
+
+/* util::DiskArgs (include/nbody/util.h) as a plain struct; the reference's defaults are
+ * center 0, vel 0, axis (0, 0, 1), inner 0, outer 250, thickness 1, central mass 4.1e6
+ * (nbody::sagittarius_mass), star mass 1 (nbody::solar_mass). */
+typedef struct nbody_disk_args
+{
+    float center[3];
+    float vel[3];
+    float axis[3];
+    float inner_radius;
+    float outer_radius;
+    float thickness;
+    float central_mass;
+    float star_mass;
+} nbody_disk_args;
+
+/* util::CubeArgs: center (unused by the reference's generator, as here), edge `size`
+ * (default 500), vel, star mass. */
+typedef struct nbody_cube_args
+{
+    float center[3];
+    float size;
+    float vel[3];
+    float star_mass;
+} nbody_cube_args;
+
+/* Fill device bodies [begin, begin + num) as util::disk (source/util.cpp:14-96) fills the
+ * range [begin, end): a central body and num - 1 stars with circular speeds, from the
+ * reference's own random stream (std::default_random_engine, seed 1, through
+ * uniform_real_distribution<float> and normal_distribution<float> as libstdc++ draws
+ * them). begin must not exceed the body count; the count grows to begin + num when that
+ * is larger. The speeds use the centre of mass and mass of the generated bodies, which is
+ * what the reference's theta = 0.5 walk of its own tree (util.cpp:81-95) folds together
+ * for every body, up to its float rounding. Replaces util::disk for a device solver. */
+int nbody_cuda_scene_disk(nbody_cuda* ctx, const nbody_disk_args* args, size_t begin, size_t num);
+
+/* Fill device bodies [begin, begin + num) as util::cube (source/util.cpp:98-126) does. */
+int nbody_cuda_scene_cube(nbody_cuda* ctx, const nbody_cube_args* args, size_t begin, size_t num);
+
 /* --- stepping (queued, asynchronous) --------------------------------------------------- */
 
 /* Accelerations for every body. Replaces GpuDevice::accelerate (source/gpu.cpp:799-841). */

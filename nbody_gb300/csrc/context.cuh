@@ -122,6 +122,10 @@ namespace nbg
     int prefetch_records(nbody_cuda* ctx, unsigned mask);
     void release_transfer(nbody_cuda* ctx);
 
+    // scenes.cu
+    int scene_disk(nbody_cuda* ctx, const nbody_disk_args* a, size_t begin, size_t num);
+    int scene_cube(nbody_cuda* ctx, const nbody_cube_args* a, size_t begin, size_t num);
+
     // direct_precise.cu
     int precise_accelerate(nbody_cuda* ctx, const nbody_step_params* p);
     int precise_integrate(nbody_cuda* ctx, const nbody_step_params* p);

@@ -141,6 +141,36 @@ namespace nbody
 
         [[nodiscard]] nbody_cuda* device() const { return _dev; }
 
+        // util::disk / util::cube (source/util.cpp:14-126) over State::bodies[begin, end),
+        // generated on the device from the reference's own random stream; state()
+        // materialises them. `args` is the reference's util::DiskArgs / CubeArgs, or any
+        // type with their fields.
+        template <class DiskArgs>
+        void disk(const size_t begin, const size_t end, const DiskArgs& args)
+        {
+            nbody_disk_args a{};
+            put3(a.center, args.center);
+            put3(a.vel, args.vel);
+            put3(a.axis, args.axis);
+            a.inner_radius = args.inner_radius;
+            a.outer_radius = args.outer_radius;
+            a.thickness = args.thickness;
+            a.central_mass = args.central_mass;
+            a.star_mass = args.star_mass;
+            generate(begin, end, [&] { return nbody_cuda_scene_disk(_dev, &a, begin, end - begin); });
+        }
+
+        template <class CubeArgs>
+        void cube(const size_t begin, const size_t end, const CubeArgs& args)
+        {
+            nbody_cube_args a{};
+            put3(a.center, args.center);
+            a.size = args.size;
+            put3(a.vel, args.vel);
+            a.star_mass = args.star_mass;
+            generate(begin, end, [&] { return nbody_cuda_scene_cube(_dev, &a, begin, end - begin); });
+        }
+
     private:
         static std::string last_error(const nbody_cuda* dev)
         {
@@ -183,6 +213,32 @@ namespace nbody
                 _host_dirty = false;
             }
             return true;
+        }
+
+        template <class V>
+        static void put3(float out[3], const V& v)
+        {
+            out[0] = v.x;
+            out[1] = v.y;
+            out[2] = v.z;
+        }
+
+        // Bring the device up to date with everything outside the range, then generate.
+        template <class F>
+        void generate(const size_t begin, const size_t end, F&& call)
+        {
+            if (begin > end || end > _state->bodies.size())
+                throw std::out_of_range("CudaSolver: generated range outside the bodies");
+            if (begin == end)
+                return;
+            if (_host_dirty || nbody_cuda_count(_dev) != _state->bodies.size())
+            {
+                check(nbody_cuda_upload_bodies(_dev, _state->bodies.data(), _state->bodies.size()), "upload");
+                _host_dirty = false;
+            }
+            check(call(), "scene generator");
+            _device_dirty = true;
+            _tree_valid = false;
         }
 
         void stepped()

@@ -12,6 +12,7 @@
 #include "nbody/bhtree.h"
 #include "nbody/body.h"
 #include "nbody/state.h"
+#include "nbody/util.h"
 #include "nbody/variant.h"
 
 namespace nbody
@@ -54,6 +55,12 @@ namespace nbody
         void update(float dt);
         void accelerate();
         void integrate(float dt);
+
+        // util::disk / util::cube (source/util.cpp:14-126) over bodies()[begin, end),
+        // generated by the active CUDA variant on the device; throws std::logic_error on a
+        // variant without a device generator and std::out_of_range outside the bodies.
+        void disk(size_t begin, size_t end, const util::DiskArgs& args = {});
+        void cube(size_t begin, size_t end, const util::CubeArgs& args = {});
 
         [[nodiscard]] const bh::Tree* tree() const;
         [[nodiscard]] std::span<const bh::Node> nodes() const;

@@ -213,6 +213,24 @@ void Sim::integrate(const float dt)
     _solver->integrate(dt);
 }
 
+void Sim::disk(const size_t begin, const size_t end, const util::DiskArgs& args)
+{
+    sync_solver();
+    auto* cuda = dynamic_cast<CudaSolver*>(_solver.get());
+    if (!cuda)
+        throw std::logic_error("Sim::disk: the active variant has no device generator");
+    cuda->disk(begin, end, args);
+}
+
+void Sim::cube(const size_t begin, const size_t end, const util::CubeArgs& args)
+{
+    sync_solver();
+    auto* cuda = dynamic_cast<CudaSolver*>(_solver.get());
+    if (!cuda)
+        throw std::logic_error("Sim::cube: the active variant has no device generator");
+    cuda->cube(begin, end, args);
+}
+
 const nbody::bh::Tree* Sim::tree() const { return _solver->tree(); }
 
 std::span<const nbody::bh::Node> Sim::nodes() const

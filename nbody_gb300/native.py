@@ -42,7 +42,7 @@ EXPORTS = (
     "nbody_cuda_system_energy", "nbody_cuda_update_graph", "nbody_cuda_direct_variant_count",
     "nbody_cuda_direct_variant", "nbody_cuda_set_direct_variant", "nbody_cuda_direct_autotune",
     "nbody_cuda_selftest_wait", "nbody_cuda_set_transfer", "nbody_cuda_transfer_info",
-    "nbody_cuda_prefetch",
+    "nbody_cuda_prefetch", "nbody_cuda_scene_disk", "nbody_cuda_scene_cube",
 )
 
 
@@ -51,6 +51,31 @@ class StepParams(C.Structure):
     _fields_ = [("dt", C.c_float), ("theta", C.c_float), ("G", C.c_float), ("eps2", C.c_float),
                 ("size", C.c_float), ("wrap", C.c_int32), ("mode", C.c_int32), ("law", C.c_int32),
                 ("precision", C.c_int32), ("tree_box", C.c_int32), ("reserved", C.c_int32 * 2)]
+
+
+class DiskArgs(C.Structure):
+    """nbody_disk_args: util::DiskArgs (include/nbody/util.h of the reference)."""
+    _fields_ = [("center", C.c_float * 3), ("vel", C.c_float * 3), ("axis", C.c_float * 3),
+                ("inner_radius", C.c_float), ("outer_radius", C.c_float), ("thickness", C.c_float),
+                ("central_mass", C.c_float), ("star_mass", C.c_float)]
+
+
+class CubeArgs(C.Structure):
+    """nbody_cube_args: util::CubeArgs."""
+    _fields_ = [("center", C.c_float * 3), ("size", C.c_float), ("vel", C.c_float * 3), ("star_mass", C.c_float)]
+
+
+def disk_args(center=(0.0, 0.0, 0.0), vel=(0.0, 0.0, 0.0), axis=(0.0, 0.0, 1.0), inner_radius=0.0,
+              outer_radius=250.0, thickness=1.0, central_mass=4.1e6, star_mass=1.0) -> DiskArgs:
+    """The reference's defaults (util.h: DiskArgs; sagittarius_mass, solar_mass)."""
+    f3 = C.c_float * 3
+    return DiskArgs(f3(*center), f3(*vel), f3(*axis), inner_radius, outer_radius, thickness, central_mass,
+                    star_mass)
+
+
+def cube_args(center=(0.0, 0.0, 0.0), size=500.0, vel=(0.0, 0.0, 0.0), star_mass=1.0) -> CubeArgs:
+    f3 = C.c_float * 3
+    return CubeArgs(f3(*center), size, f3(*vel), star_mass)
 
 
 def params(dt=0.0, theta=0.5, G=1.0, eps2=0.0, size=10000.0, wrap=False, mode=MODE_N2,
@@ -123,6 +148,8 @@ def lib() -> C.CDLL:
         "nbody_cuda_set_transfer": ([vp, C.c_int], C.c_int),
         "nbody_cuda_transfer_info": ([vp] + [C.POINTER(C.c_int)] * 3 + [C.POINTER(C.c_uint64)], C.c_int),
         "nbody_cuda_prefetch": ([vp, u], C.c_int),
+        "nbody_cuda_scene_disk": ([vp, C.POINTER(DiskArgs), sz, sz], C.c_int),
+        "nbody_cuda_scene_cube": ([vp, C.POINTER(CubeArgs), sz, sz], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -216,6 +243,16 @@ class Context:
 
     def prefetch(self, mask: int = READ_ALL):
         self.check(lib().nbody_cuda_prefetch(self.h, mask))
+
+    # --- scene generators --------------------------------------------------------
+    def scene_disk(self, num: int, begin: int = 0, **kw):
+        """util::disk on the device over bodies [begin, begin + num); kw as disk_args."""
+        a = disk_args(**kw)
+        self.check(lib().nbody_cuda_scene_disk(self.h, C.byref(a), begin, num))
+
+    def scene_cube(self, num: int, begin: int = 0, **kw):
+        a = cube_args(**kw)
+        self.check(lib().nbody_cuda_scene_cube(self.h, C.byref(a), begin, num))
 
     def reserve(self, n: int):
         self.check(lib().nbody_cuda_reserve(self.h, n))

@@ -693,3 +693,240 @@ void orc_sort_order(const uint64_t* codes, const size_t n, uint32_t* order)
     qsort(order, n, sizeof(uint32_t), orc_cmp_order);
     orc_sort_keys = NULL;
 }
+
+/* ------------------------------------------------------------------------------------
+ * Scene generators: util::compute_radius, util::disk, util::cube (source/util.cpp:9-126)
+ * and the libstdc++ (GCC 13) random machinery they draw from, restated.
+ * ---------------------------------------------------------------------------------- */
+#define ORC_MINSTD_M 2147483647u
+#define ORC_PI 3.1415926535897932384626433832795028841971693993751058209749445923078164062f
+
+typedef struct
+{
+    uint64_t x;                 /* minstd_rand0 state, seed 1 */
+    int saved_available;        /* normal_distribution's cached second value */
+    float saved;
+} orc_rng;
+
+static uint32_t orc_engine(orc_rng* g)
+{
+    g->x = (g->x * 16807u) % ORC_MINSTD_M;
+    return (uint32_t)g->x;
+}
+
+uint32_t orc_minstd_value(const uint64_t j)
+{
+    /* 16807^(j+1) mod (2^31 - 1) by square-and-multiply */
+    uint64_t e = (j + 1) % (ORC_MINSTD_M - 1), base = 16807u, r = 1;
+    while (e)
+    {
+        if (e & 1)
+            r = (r * base) % ORC_MINSTD_M;
+        base = (base * base) % ORC_MINSTD_M;
+        e >>= 1;
+    }
+    return (uint32_t)r;
+}
+
+/* generate_canonical<float, 24>: one engine value; sum / 2^31 where 2^31 is the engine's
+ * range 2^31 - 2 rounded to float. */
+static float orc_canonical(orc_rng* g)
+{
+    const float sum = (float)(orc_engine(g) - 1u) * 1.0f;
+    const float tmp = (float)(1.0L * (long double)(ORC_MINSTD_M - 1u));
+    float ret = sum / tmp;
+    if (ret >= 1.0f)
+        ret = nextafterf(1.0f, 0.0f);
+    return ret;
+}
+
+static float orc_uniform(orc_rng* g, const float a, const float b)
+{
+    return (orc_canonical(g) * (b - a)) + a;
+}
+
+/* normal_distribution<float>::operator(): Marsaglia polar method. */
+static float orc_normal(orc_rng* g, const float mean, const float stddev)
+{
+    float ret;
+    if (g->saved_available)
+    {
+        g->saved_available = 0;
+        ret = g->saved;
+    }
+    else
+    {
+        float x, y, r2;
+        do
+        {
+            x = (float)((double)(2.0f * orc_canonical(g)) - 1.0);
+            y = (float)((double)(2.0f * orc_canonical(g)) - 1.0);
+            r2 = x * x + y * y;
+        } while ((double)r2 > 1.0 || (double)r2 == 0.0);
+        const float mult = sqrtf(-2 * logf(r2) / r2);
+        g->saved = x * mult;
+        g->saved_available = 1;
+        ret = y * mult;
+    }
+    return ret * stddev + mean;
+}
+
+float orc_compute_radius(const float mass, const float density)
+{
+    return powf((3.f * ORC_PI * mass) / (4.f * density), 1.f / 3.f);
+}
+
+static void orc_put_body(float* b, const float p[3], const float radius, const float v[3], const float mass)
+{
+    b[0] = p[0]; b[1] = p[1]; b[2] = p[2]; b[3] = radius;
+    b[4] = v[0]; b[5] = v[1]; b[6] = v[2]; b[7] = mass;
+    b[8] = 0.f; b[9] = 0.f; b[10] = 0.f; b[11] = 0.f;
+}
+
+static void orc_norm3(float v[3])
+{
+    const float s = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+    v[0] = v[0] / s;
+    v[1] = v[1] / s;
+    v[2] = v[2] / s;
+}
+
+static void orc_cross3(const float a[3], const float b[3], float out[3])
+{
+    out[0] = (a[1] * b[2]) - (a[2] * b[1]);
+    out[1] = (a[2] * b[0]) - (a[0] * b[2]);
+    out[2] = (a[0] * b[1]) - (a[1] * b[0]);
+}
+
+/* The star loop of util::disk (util.cpp:52-79) for stars [1, num), writing bodies whose
+ * index lies in [first, last) (all when last == 0) and inserting every star into `tree`
+ * when one is given. */
+static void orc_disk_stars(float* bodies, const size_t num, const float a[14], const size_t first,
+                           const size_t last, orc_tree* tree)
+{
+    const float center[3] = { a[0], a[1], a[2] };
+    const float axis[3] = { a[6], a[7], a[8] };
+    float inner = a[9], outer = a[10];
+    const float thickness = a[11], central_mass = a[12], star_mass = a[13];
+    const float center_radius = orc_compute_radius(central_mass, 1e2f);
+    outer = outer < center_radius ? center_radius : outer;      /* std::max */
+    inner = inner < center_radius ? center_radius : inner;
+
+    orc_rng g = { 1u, 0, 0.f };
+    const float c0[3] = { copysignf(axis[2], axis[0]), copysignf(axis[2], axis[1]),
+                          -copysignf(axis[0], axis[2]) - copysignf(axis[1], axis[2]) };
+    float c1[3];
+    orc_cross3(axis, c0, c1);
+
+    for (size_t i = 1; i < num; ++i)
+    {
+        const float t = (float)i / (float)(num - 1);
+        const float angle = t * 2.f * ORC_PI;
+        /* the unqualified sqrt of a float is ::sqrt(double) */
+        const float dist = (float)((double)inner + (sqrt((double)orc_uniform(&g, 0.f, 1.f)) * (double)(outer - inner)));
+        const float disp = ((outer - dist) / outer) * (thickness * center_radius) * orc_normal(&g, 0.f, .5f);
+        if (!tree && (i < first || (last && i >= last)))
+            continue;
+        const float s = sinf(angle), c = cosf(angle);
+        float s0[3] = { (s * c0[0]) + (c * c1[0]), (s * c0[1]) + (c * c1[1]), (s * c0[2]) + (c * c1[2]) };
+        orc_norm3(s0);
+        float s1[3];
+        orc_cross3(axis, s0, s1);
+        orc_norm3(s1);
+        const float p[3] = { (center[0] + (s0[0] * dist)) + (axis[0] * disp),
+                             (center[1] + (s0[1] * dist)) + (axis[1] * disp),
+                             (center[2] + (s0[2] * dist)) + (axis[2] * disp) };
+        if (i >= first && (!last || i < last))
+            orc_put_body(bodies + 12 * i, p, orc_compute_radius(star_mass, 1e2f), s1, star_mass);
+        if (tree)
+            orc_tree_insert(tree, p[0], p[1], p[2], star_mass);
+    }
+}
+
+void orc_disk_positions(float* bodies, const size_t num, const float a[14], const size_t first, const size_t last)
+{
+    orc_disk_stars(bodies, num, a, first ? first : 1, last, NULL);
+}
+
+void orc_disk(float* bodies, const size_t num, const float a[14])
+{
+    if (num == 0)
+        return;
+    const float center[3] = { a[0], a[1], a[2] };
+    const float vel[3] = { a[3], a[4], a[5] };
+    const float outer = a[10], central_mass = a[12];
+
+    /* the tree's edge is twice the outer radius as given, before the clamp */
+    orc_tree* tree = orc_tree_new(1.f);
+    orc_tree_clear(tree, center[0], center[1], center[2], 2.f * outer);
+
+    const float center_radius = orc_compute_radius(central_mass, 1e2f);
+    const float zero[3] = { 0.f, 0.f, 0.f };
+    orc_put_body(bodies, center, center_radius, zero, central_mass);
+    orc_tree_insert(tree, center[0], center[1], center[2], central_mass);
+
+    orc_disk_stars(bodies, num, a, 1, 0, tree);
+
+    /* circular speeds: Tree::apply(pos, visitor, 0.5) (bhtree.cpp:97-138) with the
+     * running centre-of-mass visitor of util.cpp:84-90 */
+    const orc_node* nodes = tree->nodes;
+    const size_t count = tree->count;
+    const float theta_sq = .5f * .5f;
+    for (size_t k = 0; k < num; ++k)
+    {
+        float* b = bodies + 12 * k;
+        float com[3] = { 0.f, 0.f, 0.f }, mass = 0.f;
+        uint32_t idx = 0;
+        do
+        {
+            const orc_node* nd = &nodes[idx];
+            if (nd->mass == 0)
+            {
+                idx = nd->next;
+                continue;
+            }
+            int apply = nd->children == 0;
+            if (!apply)
+            {
+                const float node_size_sq = nd->size * nd->size;
+                const float dx = nd->comx - b[0], dy = nd->comy - b[1], dz = nd->comz - b[2];
+                apply = ((dx * dx + dy * dy) + dz * dz) > node_size_sq * theta_sq;
+            }
+            if (apply)
+            {
+                const float tot = mass + nd->mass;
+                com[0] = ((com[0] * mass) + (nd->comx * nd->mass)) / tot;
+                com[1] = ((com[1] * mass) + (nd->comy * nd->mass)) / tot;
+                com[2] = ((com[2] * mass) + (nd->comz * nd->mass)) / tot;
+                mass += nd->mass;
+                idx = nd->next;
+                continue;
+            }
+            idx = nd->children;
+        } while (0 < idx && idx < count);
+        const float d[3] = { com[0] - b[0], com[1] - b[1], com[2] - b[2] };
+        const float dist = sqrtf((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+        const float speed = sqrtf(1.f * mass / dist);
+        b[4] = vel[0] + (b[4] * speed);
+        b[5] = vel[1] + (b[5] * speed);
+        b[6] = vel[2] + (b[6] * speed);
+    }
+    orc_tree_free(tree);
+}
+
+void orc_cube(float* bodies, const size_t num, const float a[8])
+{
+    const float size = a[3];
+    const float vel[3] = { a[4], a[5], a[6] };
+    const float star_mass = a[7];
+    orc_rng g = { 1u, 0, 0.f };
+    const float lo = (float)(-.5 * (double)size), hi = (float)(.5 * (double)size);
+    for (size_t i = 0; i < num; ++i)
+    {
+        float p[3];
+        p[0] = orc_uniform(&g, lo, hi);
+        p[1] = orc_uniform(&g, lo, hi);
+        p[2] = orc_uniform(&g, lo, hi);
+        orc_put_body(bodies + 12 * i, p, orc_compute_radius(star_mass, 1e2f), vel, star_mass);
+    }
+}

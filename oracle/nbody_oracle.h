@@ -98,6 +98,26 @@ void orc_morton63(const float* xyz, size_t stride, size_t n, const double lo[3],
 /* Stable order by (code, index). */
 void orc_sort_order(const uint64_t* codes, size_t n, uint32_t* order);
 
+/* --- scene generators (source/util.cpp:9-126) ------------------------------------- */
+/* The reference's random stream, restated: std::default_random_engine of libstdc++ (GCC 13)
+ * is minstd_rand0, x <- 16807 x mod (2^31 - 1), seed 1; generate_canonical<float, 24>
+ * takes one engine value (the range 2^31 - 2 holds >= 24 bits): float(x - 1) / 2^31,
+ * clamped below 1; uniform_real_distribution<float>(a, b) = canonical * (b - a) + a;
+ * normal_distribution<float> is the Marsaglia polar method with the second value saved. */
+uint32_t orc_minstd_value(uint64_t j);      /* the j-th value (from 0) the engine returns */
+float orc_compute_radius(float mass, float density);
+/* util::disk over bodies[0, num): a[] = center[3], vel[3], axis[3], inner, outer,
+ * thickness, central mass, star mass. Velocities from the reference's own walk: a tree
+ * rooted at the centre with edge 2 * outer (before the clamp), theta 0.5, folding the
+ * applied nodes into a running centre of mass (util.cpp:81-95). */
+void orc_disk(float* bodies, size_t num, const float a[14]);
+/* The star positions of util::disk for stars [first, last) only (last 0: all), with the
+ * random stream drawn in full up to them and no velocity pass: a fast check of any tail
+ * of a large disk. Writes only those bodies (velocities are the unit directions). */
+void orc_disk_positions(float* bodies, size_t num, const float a[14], size_t first, size_t last);
+/* util::cube over bodies[0, num): a[] = center[3], size, vel[3], star mass. */
+void orc_cube(float* bodies, size_t num, const float a[8]);
+
 /* Threads this process would use by default (online CPUs). */
 int orc_default_threads(void);
 

@@ -69,6 +69,13 @@ def lib():
         L.orc_morton63.argtypes = [_F, _SZ, _SZ, _D, C.c_double, _U64]
         L.orc_sort_order.argtypes = [_U64, _SZ, _U32]
         L.orc_default_threads.restype = C.c_int
+        L.orc_minstd_value.argtypes = [C.c_uint64]
+        L.orc_minstd_value.restype = C.c_uint32
+        L.orc_compute_radius.argtypes = [C.c_float, C.c_float]
+        L.orc_compute_radius.restype = C.c_float
+        L.orc_disk.argtypes = [_F, _SZ, _F]
+        L.orc_cube.argtypes = [_F, _SZ, _F]
+        L.orc_disk_positions.argtypes = [_F, _SZ, _F, _SZ, _SZ]
         _lib = L
     return _lib
 
@@ -99,6 +106,8 @@ def ref_lib():
         L.ref_insert_points.restype = _SZ
         L.ref_disk.argtypes = [_F, _SZ, C.c_float, C.c_float, C.c_float, C.c_float]
         L.ref_cube.argtypes = [_F, _SZ]
+        L.ref_disk_args.argtypes = [_F, _SZ, _SZ, _SZ, _F]
+        L.ref_cube_args.argtypes = [_F, _SZ, _SZ, _SZ, _F]
         _ref = L
     return _ref
 
@@ -309,4 +318,61 @@ def ref_disk(n, center=(0.0, 0.0, 0.0), outer_radius=100.0):
 def ref_cube(n):
     b = np.zeros((n, 12), np.float32)
     ref_lib().ref_cube(_p(b, _F), n)
+    return b
+
+
+# --- scene generators (source/util.cpp) ---------------------------------------------------
+
+DISK_DEFAULTS = dict(center=(0.0, 0.0, 0.0), vel=(0.0, 0.0, 0.0), axis=(0.0, 0.0, 1.0), inner_radius=0.0,
+                     outer_radius=250.0, thickness=1.0, central_mass=4.1e6, star_mass=1.0)
+CUBE_DEFAULTS = dict(center=(0.0, 0.0, 0.0), size=500.0, vel=(0.0, 0.0, 0.0), star_mass=1.0)
+
+
+def disk_arg_array(**kw):
+    """util::DiskArgs as the 14 floats the oracle and the reference driver take."""
+    a = dict(DISK_DEFAULTS, **kw)
+    return np.array([*a["center"], *a["vel"], *a["axis"], a["inner_radius"], a["outer_radius"],
+                     a["thickness"], a["central_mass"], a["star_mass"]], np.float32)
+
+
+def cube_arg_array(**kw):
+    a = dict(CUBE_DEFAULTS, **kw)
+    return np.array([*a["center"], a["size"], *a["vel"], a["star_mass"]], np.float32)
+
+
+def minstd_value(j: int) -> int:
+    return int(lib().orc_minstd_value(j))
+
+
+def disk(num: int, **kw) -> np.ndarray:
+    """The oracle's util::disk over a fresh array of num bodies."""
+    b = np.zeros((num, 12), np.float32)
+    lib().orc_disk(_p(b, _F), num, _p(disk_arg_array(**kw), _F))
+    return b
+
+
+def disk_positions(num: int, first: int, last: int, **kw) -> np.ndarray:
+    """Bodies [first, last) of util::disk(num) without the velocity pass: positions,
+    radius and mass as the reference writes them, velocity the unit direction."""
+    b = np.zeros((num, 12), np.float32)
+    lib().orc_disk_positions(_p(b, _F), num, _p(disk_arg_array(**kw), _F), first, last)
+    return b[first:last]
+
+
+def cube(num: int, **kw) -> np.ndarray:
+    b = np.zeros((num, 12), np.float32)
+    lib().orc_cube(_p(b, _F), num, _p(cube_arg_array(**kw), _F))
+    return b
+
+
+def ref_disk_range(bodies: np.ndarray, begin: int, num: int, **kw) -> np.ndarray:
+    """The reference's util::disk over bodies[begin, begin + num) of a copy of `bodies`."""
+    b = np.ascontiguousarray(bodies, np.float32).copy()
+    ref_lib().ref_disk_args(_p(b, _F), len(b), begin, num, _p(disk_arg_array(**kw), _F))
+    return b
+
+
+def ref_cube_range(bodies: np.ndarray, begin: int, num: int, **kw) -> np.ndarray:
+    b = np.ascontiguousarray(bodies, np.float32).copy()
+    ref_lib().ref_cube_args(_p(b, _F), len(b), begin, num, _p(cube_arg_array(**kw), _F))
     return b

@@ -150,4 +150,36 @@ extern "C"
         if (n)
             std::memcpy(bodies, bs.data(), n * sizeof(nbody::Body));
     }
+
+    // util::disk over bodies[begin, begin + num) of an n-body array, every DiskArgs field
+    // given: center[3], vel[3], axis[3], inner, outer, thickness, central mass, star mass.
+    void ref_disk_args(float* bodies, size_t n, size_t begin, size_t num, const float* a)
+    {
+        std::vector<nbody::Body> bs(n);
+        if (n)
+            std::memcpy(bs.data(), bodies, n * sizeof(nbody::Body));
+        nbody::util::DiskArgs args{ .center = { a[0], a[1], a[2] }, .vel = { a[3], a[4], a[5] },
+                                    .axis = { a[6], a[7], a[8] } };
+        args.inner_radius = a[9];
+        args.outer_radius = a[10];
+        args.thickness = a[11];
+        args.central_mass = a[12];
+        args.star_mass = a[13];
+        nbody::util::disk(bs.begin() + begin, bs.begin() + begin + num, args);
+        if (n)
+            std::memcpy(bodies, bs.data(), n * sizeof(nbody::Body));
+    }
+
+    // util::cube over bodies[begin, begin + num): center[3], size, vel[3], star mass.
+    void ref_cube_args(float* bodies, size_t n, size_t begin, size_t num, const float* a)
+    {
+        std::vector<nbody::Body> bs(n);
+        if (n)
+            std::memcpy(bs.data(), bodies, n * sizeof(nbody::Body));
+        nbody::util::CubeArgs args{ .center = { a[0], a[1], a[2] }, .size = a[3], .vel = { a[4], a[5], a[6] } };
+        args.star_mass = a[7];
+        nbody::util::cube(bs.begin() + begin, bs.begin() + begin + num, args);
+        if (n)
+            std::memcpy(bodies, bs.data(), n * sizeof(nbody::Body));
+    }
 }

@@ -499,6 +499,81 @@ TEST_CASE(the_exported_tree_walks_like_the_reference)
     CHECK(inter > 0 && worst < 1e-2f);
 }
 
+// util::disk appended after existing bodies, as test_variant.cpp:150-160 grows a scene:
+// generated on the device by every CUDA variant, against the oracle's util::disk.
+TEST_CASE(every_variant_generates_the_reference_disk_on_the_device)
+{
+    const size_t keep = 257, added = 3001;
+    const float args14[14] = { 1.f, 2.f, 3.f, 0.f, 0.5f, 0.f, 0.f, 0.f, 1.f, 0.f, 100.f, 1.f, 4.1e6f, 1.f };
+    std::vector<float> want(12 * added);
+    orc_disk(want.data(), added, args14);
+    for (Variant v : kCuda)
+    {
+        Sim sim(v);
+        seed_disk(sim, keep);
+        const std::vector<Body> before = sim.bodies();
+        sim.mutable_bodies().resize(keep + added);
+        nbody::util::DiskArgs args{ .center = { 1.f, 2.f, 3.f }, .vel = { 0.f, 0.5f, 0.f } };
+        args.outer_radius = 100.f;
+        sim.disk(keep, keep + added, args);
+        const std::vector<Body>& got = sim.bodies();
+        CHECK(got.size() == keep + added);
+        CHECK(std::memcmp(got.data(), before.data(), keep * sizeof(Body)) == 0);
+        size_t exact = 0;
+        float worst_pos = 0.f, worst_vel = 0.f;
+        for (size_t i = 0; i < added; ++i)
+        {
+            const Body& g = got[keep + i];
+            Body w;
+            std::memcpy(&w, want.data() + 12 * i, sizeof w);
+            CHECK(g.mass == w.mass && g.radius == w.radius);
+            exact += g.pos == w.pos;
+            worst_pos = std::max(worst_pos, (g.pos - w.pos).size());
+            if (w.vel.size() > 0.f)
+                worst_vel = std::max(worst_vel, (g.vel - w.vel).size() / w.vel.size());
+        }
+        CHECK(worst_pos <= 1e-6f * 103.f);
+        CHECK(exact * 10 >= added * 9);
+        CHECK(worst_vel <= 1e-5f);
+        // and it steps from there like any other scene
+        sim.update(1.f / 120.f);
+        CHECK(std::isfinite(sim.bodies()[keep + added - 1].pos.x));
+    }
+}
+
+TEST_CASE(every_variant_generates_the_reference_cube_on_the_device)
+{
+    const size_t n = 4096;
+    const float args8[8] = { 0.f, 0.f, 0.f, 500.f, 0.f, 0.f, 0.f, 1.f };
+    std::vector<float> want(12 * n);
+    orc_cube(want.data(), n, args8);
+    for (Variant v : kCuda)
+    {
+        Sim sim(v);
+        sim.mutable_bodies().resize(n);
+        sim.cube(0, n);
+        const std::vector<Body>& got = sim.bodies();
+        for (size_t i = 0; i < n; ++i)
+            CHECK(std::memcmp(&got[i], want.data() + 12 * i, 44) == 0);
+    }
+}
+
+TEST_CASE(a_generated_range_outside_the_bodies_throws)
+{
+    Sim sim(Variant::CudaBruteForce);
+    sim.mutable_bodies().resize(10);
+    bool threw = false;
+    try
+    {
+        sim.disk(5, 11);
+    }
+    catch (const std::out_of_range&)
+    {
+        threw = true;
+    }
+    CHECK(threw);
+}
+
 TEST_CASE(a_solver_constructed_without_a_device_throws_a_reason)
 {
     // The probe result, not a fault: with the injected no-device fault the constructor throws

@@ -12,6 +12,8 @@ oracle/build_oracle.py) and records its inputs and outputs:
   accelerations and the octree node array (detail::build_tree, tree.h:14-29).
 * ``bhtree_cases.npz`` -- the insertion sequences of tests/source/test_bhtree.cpp:30-142
   and the node arrays the reference builds for them.
+* ``scenes.npz`` -- util::disk and util::cube (util.cpp:14-126) over body ranges of
+  arrays with other bodies around them, for the argument sets in DISK_CASES / CUBE_CASES.
 
 Usage: ``python tests/golden/make_golden.py`` (needs the reference checkout; the
 fixtures are committed so the tests never need it).
@@ -56,7 +58,45 @@ def main() -> None:
         out[f"{name}_points"] = pts
         out[f"{name}_nodes"] = O.ref_insert_points(pts, (0, 0, 0), 100.0).view(np.uint8)
     np.savez_compressed(HERE / "bhtree_cases.npz", **out)
+    np.savez_compressed(HERE / "scenes.npz", **scene_fixtures())
     print("fixtures written to", HERE)
+
+
+# util::disk / util::cube argument sets: (total bodies, begin, num, keyword arguments)
+DISK_CASES = {
+    "defaults": (4097, 0, 4097, {}),
+    "tilted": (1000, 0, 1000, dict(center=(10.0, -5.0, 3.0), vel=(1.0, 2.0, 3.0), axis=(0.0, 0.6, 0.8),
+                                   inner_radius=50.0, outer_radius=300.0, thickness=2.0, central_mass=1e5,
+                                   star_mass=2.0)),
+    "one_star": (2, 0, 2, dict(outer_radius=100.0)),
+    "central_only": (1, 0, 1, {}),
+    "appended": (1001, 300, 701, dict(outer_radius=100.0, axis=(1.0, 0.0, 0.0))),
+    "clamped_radii": (777, 0, 777, dict(outer_radius=10.0, axis=(0.0, 0.0, -1.0))),
+}
+CUBE_CASES = {
+    "defaults": (3000, 0, 3000, {}),
+    "moving": (500, 100, 300, dict(center=(5.0, 5.0, 5.0), size=100.0, vel=(0.5, 0.0, -1.0), star_mass=3.0)),
+}
+
+
+def scene_fixtures() -> dict:
+    out = {}
+    for kind, cases, run, args in (("disk", DISK_CASES, O.ref_disk_range, O.disk_arg_array),
+                                   ("cube", CUBE_CASES, O.ref_cube_range, O.cube_arg_array)):
+        for name, (n, begin, num, kw) in cases.items():
+            before = scene_prefix(n)
+            after = run(before, begin, num, **kw)
+            out[f"{kind}_{name}_bodies"] = after[begin:begin + num]
+            out[f"{kind}_{name}_args"] = args(**kw)
+            out[f"{kind}_{name}_range"] = np.array([n, begin, num], np.int64)
+            assert np.array_equal(np.delete(after, np.s_[begin:begin + num], 0),
+                                  np.delete(before, np.s_[begin:begin + num], 0)), "bodies outside the range moved"
+    return out
+
+
+def scene_prefix(n: int) -> np.ndarray:
+    """The bodies around a generated range: a fixed pattern the generators must not touch."""
+    return (np.arange(n * 12, dtype=np.float32).reshape(n, 12) % 97.0) - 48.0
 
 
 if __name__ == "__main__":
