@@ -29,6 +29,8 @@ Printed JSON line (rank 0):
   configs         configs 1 (N = 4096 Plummer, 100 steps) and 2 (2 x 131072 Plummer BH).
   scene_generators util::disk and util::cube on the device at N = 16,777,216, against the
                   reference's serial generator on 1,048,576 bodies.
+  ray_query       Tree::query over the exported tree of 1,048,576 bodies: picking rays
+                  and full walks per second, against the walk on one host core.
   cpu_baseline    the reference's CPU brute force (oracle/_ref, built from the reference's
                   sources) where it loads, else the oracle's C restatement, on all host
                   cores, timed on a bounded sample of targets against all N sources.
@@ -281,6 +283,7 @@ def _bench_gpu(args, stream):
         extra["configs"]["config4_batched"] = bench_batched(torch, stream, flush, native, scenes,
                                                             float(N) * N / (acc_ms * 1e-3))
         extra["scene_generators"] = bench_scenes(torch, stream, native)
+        extra["ray_query"] = bench_query(native, scenes)
 
     line = None
     if rank == 0:
@@ -530,6 +533,43 @@ def bench_scenes(torch, stream, native, reps=5):
                            "kind": "reference" if ref else "port",
                            "sample": "util::disk, 1,048,576 bodies (the reference's generator is serial)"}
     out["disk_speedup_vs_cpu"] = out["disk"]["bodies_per_s"] / out["cpu_baseline"]["value"]
+    return out
+
+
+def bench_query(native, scenes):
+    """Tree::query for many rays over the exported Barnes-Hut tree of a 1,048,576-body
+    Plummer sphere: picking rays (stop at the first body leaf) and full walks, through the
+    C ABI with host ray and hit arrays, against the oracle's walk on one host core."""
+    from oracle import oracle as O
+    n = 1 << 20
+    b = scenes.plummer(n, seed=2)
+    g = np.random.default_rng(1)
+    out = {"n_bodies": n}
+    with native.Context() as ctx:
+        ctx.upload_bodies(b)
+        ctx.accelerate(native.params(mode=native.MODE_NLOGN, theta=0.5, law=native.LAW_SOFTENED, eps2=1e-4,
+                                     size=0.0, tree_box=1))
+        t0 = time.perf_counter()
+        nodes = ctx.tree_export()
+        out["tree_nodes"] = len(nodes)
+        out["export_ms"] = (time.perf_counter() - t0) * 1e3
+        for name, nr, stop, mh in (("picking", 1 << 20, native.QUERY_FIRST_BODY, 64),
+                                   ("full_walk", 1 << 16, native.QUERY_ALL, 256)):
+            rays = np.concatenate([g.normal(0, 3, (nr, 3)), g.normal(0, 1, (nr, 3))], 1).astype(np.float32)
+            ctx.tree_query(rays[:1024], stop, mh)
+            t0 = time.perf_counter()
+            _, counts = ctx.tree_query(rays, stop, mh)
+            t = time.perf_counter() - t0
+            k = 2000
+            t0 = time.perf_counter()
+            for r in range(k):
+                O.tree_query(nodes, rays[r], stop, mh)
+            tc = time.perf_counter() - t0
+            out[name] = {"rays": nr, "ms": t * 1e3, "rays_per_s": nr / t, "mean_nodes_visited": float(counts.mean()),
+                         "cpu_baseline": {"value": k / tc, "unit": "rays/s", "cores": 1, "kind": "port",
+                                          "sample": "%d rays, the restated Tree::query walk" % k},
+                         "speedup_vs_cpu": (nr / t) / (k / tc)}
+    out["note"] = "wall clock of nbody_cuda_tree_query including the ray upload and hit download"
     return out
 
 

@@ -305,6 +305,27 @@ int nbody_cuda_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* cod
  * tree-building variant (source/solvers/cpu_barnes_hut.h:46, sim.cpp:329-335). */
 int nbody_cuda_tree_export(nbody_cuda* ctx, void* nodes, size_t max_nodes, size_t* count);
 
+/* When a ray query stops (the visitor's answer in Tree::query). */
+enum
+{
+    NBODY_QUERY_ALL = 0,            /* visit every node the ray meets */
+    NBODY_QUERY_FIRST_BODY = 1      /* stop after the first met leaf that holds mass (picking) */
+};
+
+/* Tree::query (source/bhtree.cpp:153-173) for nrays rays at once. rays: 6 floats per ray,
+ * origin xyz then direction xyz (nbody::Ray, include/nbody/ray.h). The tree is `count`
+ * bh::Node records at `nodes` (any reference tree, e.g. Tree::nodes()), or, when nodes is
+ * NULL, the context's last Barnes-Hut tree as nbody_cuda_tree_export gives it. Per ray the
+ * walk visits, in the reference's order, the nodes whose bounds the ray meets
+ * (Bounds::ray_intersect, bounds.h:64-133), descending into each met node. Past a node the
+ * ray misses it moves to that node's `next`: the reference's loop stays on such a node
+ * and never ends, so the two agree wherever the reference's walk ends. hits[r * max_hits
+ * ...] receives ray r's first max_hits visited node indices and counts[r] how many it
+ * visited. A malformed node array (a link out of range, a cycle) stops the walk and
+ * returns NBODY_ERR_CUDA. Synchronous. */
+int nbody_cuda_tree_query(nbody_cuda* ctx, const void* nodes, size_t count, const float* rays, size_t nrays,
+                          int stop, uint32_t* hits, size_t max_hits, uint32_t* counts);
+
 /* --- direct-sum kernel shapes ---------------------------------------------------------------- */
 
 /* Number of instantiated direct-sum kernel shapes; describe one (targets per thread, threads

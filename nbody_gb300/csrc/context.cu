@@ -253,6 +253,7 @@ void nbody_cuda_destroy(nbody_cuda* ctx)
     release_precise(ctx);
     release_batch(ctx);
     release_transfer(ctx);
+    release_query(ctx);
     if (ctx->graph)
         cudaGraphExecDestroy(ctx->graph);
     cudaFree(ctx->pm);

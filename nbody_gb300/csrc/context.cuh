@@ -90,6 +90,14 @@ struct nbody_cuda
     std::vector<unsigned char> tree_export;
     uint64_t tree_export_id = 0;
 
+    // Ray queries (query.cu): the node array on the device (the exported tree while
+    // query_nodes_id matches its build) and the rays / hits / counts buffers.
+    void* query_nodes = nullptr;
+    size_t query_nodes_cap = 0;
+    uint64_t query_nodes_id = 0;
+    void* query_buf = nullptr;
+    size_t query_buf_cap = 0;
+
     int force_variant = -1;     // pins the direct-sum (T, block) table entry when >= 0
     nbg::DirectPlan last_plan{};
     uint64_t launches = 0;
@@ -121,6 +129,11 @@ namespace nbg
     int upload_records(nbody_cuda* ctx, const void* bodies, size_t n);
     int prefetch_records(nbody_cuda* ctx, unsigned mask);
     void release_transfer(nbody_cuda* ctx);
+
+    // query.cu
+    int tree_query(nbody_cuda* ctx, const void* nodes, size_t count, const float* rays, size_t nrays, int stop,
+                   uint32_t* hits, size_t max_hits, uint32_t* counts);
+    void release_query(nbody_cuda* ctx);
 
     // scenes.cu
     int scene_disk(nbody_cuda* ctx, const nbody_disk_args* a, size_t begin, size_t num);

@@ -20,6 +20,7 @@ LAW_CUTOFF, LAW_SOFTENED = 0, 1
 PREC_FP32, PREC_COMPENSATED, PREC_FP64 = 0, 1, 2
 LAYOUT_SOA, LAYOUT_AOS = 0, 1
 READ_POSITIONS, READ_VELOCITIES, READ_ACCELERATIONS, READ_ALL = 1, 2, 4, 7
+QUERY_ALL, QUERY_FIRST_BODY = 0, 1
 TRANSFER_AUTO, TRANSFER_STAGED, TRANSFER_MAPPED, TRANSFER_DIRECT = 0, 1, 2, 3
 
 # bh::Node (include/nbody/bhtree.h of the reference): bounds centre, size, com, mass, links
@@ -42,7 +43,7 @@ EXPORTS = (
     "nbody_cuda_system_energy", "nbody_cuda_update_graph", "nbody_cuda_direct_variant_count",
     "nbody_cuda_direct_variant", "nbody_cuda_set_direct_variant", "nbody_cuda_direct_autotune",
     "nbody_cuda_selftest_wait", "nbody_cuda_set_transfer", "nbody_cuda_transfer_info",
-    "nbody_cuda_prefetch", "nbody_cuda_scene_disk", "nbody_cuda_scene_cube",
+    "nbody_cuda_prefetch", "nbody_cuda_scene_disk", "nbody_cuda_scene_cube", "nbody_cuda_tree_query",
 )
 
 
@@ -150,6 +151,7 @@ def lib() -> C.CDLL:
         "nbody_cuda_prefetch": ([vp, u], C.c_int),
         "nbody_cuda_scene_disk": ([vp, C.POINTER(DiskArgs), sz, sz], C.c_int),
         "nbody_cuda_scene_cube": ([vp, C.POINTER(CubeArgs), sz, sz], C.c_int),
+        "nbody_cuda_tree_query": ([vp, vp, sz, vp, sz, C.c_int, vp, sz, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -243,6 +245,20 @@ class Context:
 
     def prefetch(self, mask: int = READ_ALL):
         self.check(lib().nbody_cuda_prefetch(self.h, mask))
+
+    # --- ray query ---------------------------------------------------------------
+    def tree_query(self, rays: np.ndarray, stop: int = QUERY_ALL, max_hits: int = 64,
+                   nodes: np.ndarray | None = None):
+        """Tree::query for every ray (rows of origin xyz, direction xyz) over `nodes`
+        (NODE_DTYPE) or the last Barnes-Hut tree: (hits (nrays, max_hits), counts)."""
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        hits = np.zeros((len(r), max_hits), np.uint32)
+        counts = np.zeros(len(r), np.uint32)
+        nd = None if nodes is None else np.ascontiguousarray(nodes)
+        self.check(lib().nbody_cuda_tree_query(self.h, None if nd is None else C.c_void_p(nd.ctypes.data),
+                                               0 if nd is None else len(nd), _ptr(r), len(r), stop,
+                                               _ptr(hits), max_hits, _ptr(counts)))
+        return hits, counts
 
     # --- scene generators --------------------------------------------------------
     def scene_disk(self, num: int, begin: int = 0, **kw):

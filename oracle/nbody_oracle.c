@@ -930,3 +930,75 @@ void orc_cube(float* bodies, const size_t num, const float a[8])
         orc_put_body(bodies + 12 * i, p, orc_compute_radius(star_mass, 1e2f), vel, star_mass);
     }
 }
+
+/* ------------------------------------------------------------------------------------
+ * Tree::query (source/bhtree.cpp:153-173) with Bounds::ray_intersect
+ * (include/nbody/bounds.h:64-133).
+ * ---------------------------------------------------------------------------------- */
+
+/* ray_intersect_coord<i> with length = FLT_MAX (only a hit lowers it, and ray_intersect
+ * returns on the first hit). */
+static int orc_face(const float o[3], const float d[3], const float c[3], const float s, const int i)
+{
+    const int j = (i + 1) % 3, k = (i + 2) % 3;
+    float t;
+    if (d[i] < -FLT_EPSILON)
+        t = (c[i] + s - o[i]) / d[i];
+    else if (d[i] > FLT_EPSILON)
+        t = (c[i] - s - o[i]) / d[i];
+    else
+        return 0;
+    if (!(t < FLT_MAX))
+        return 0;
+    const float p[3] = { o[0] + (d[0] * t), o[1] + (d[1] * t), o[2] + (d[2] * t) };
+    return p[j] > c[j] - s && p[j] < c[j] + s && p[k] > c[k] - s && p[k] < c[k] + s;
+}
+
+static int orc_ray_meets(const orc_node* n, const float ray[6])
+{
+    const float c[3] = { n->cx, n->cy, n->cz };
+    const float s = n->size;
+    int inside = 1;
+    for (int i = 0; i < 3; ++i)
+        if (ray[i] < c[i] - s || ray[i] > c[i] + s)
+        {
+            inside = 0;
+            break;
+        }
+    if (inside)
+        return 1;
+    return orc_face(ray, ray + 3, c, s, 0) || orc_face(ray, ray + 3, c, s, 1) || orc_face(ray, ray + 3, c, s, 2);
+}
+
+size_t orc_tree_query(const orc_node* nodes, const size_t count, const float ray[6], const int stop,
+                      uint32_t* hits, const size_t max_hits, int* missed)
+{
+    size_t visited = 0, steps = 0;
+    uint32_t idx = 0;
+    if (missed)
+        *missed = 0;
+    if (!count)
+        return 0;
+    do
+    {
+        if (idx >= count || ++steps > count)
+            break;      /* a malformed array */
+        const orc_node* nd = &nodes[idx];
+        if (orc_ray_meets(nd, ray))
+        {
+            if (visited < max_hits)
+                hits[visited] = idx;
+            ++visited;
+            if (stop == 1 && nd->children == 0 && nd->mass != 0)
+                break;
+            idx = nd->children ? nd->children : nd->next;
+        }
+        else
+        {
+            if (missed)
+                *missed = 1;
+            idx = nd->next;
+        }
+    } while (idx != 0);
+    return visited;
+}

@@ -118,6 +118,15 @@ void orc_disk_positions(float* bodies, size_t num, const float a[14], size_t fir
 /* util::cube over bodies[0, num): a[] = center[3], size, vel[3], star mass. */
 void orc_cube(float* bodies, size_t num, const float a[8]);
 
+/* --- ray query (source/bhtree.cpp:153-173) ------------------------------------------ */
+/* Tree::query over a reference node array for one ray (origin xyz, direction xyz).
+ * stop 0 visits every node the ray meets; stop 1 ends after the first met leaf with mass.
+ * Writes the first max_hits visited indices, returns how many were visited. At a node the
+ * ray misses the walk moves to its next and *missed is set: there the reference's loop
+ * would not advance and never ends. */
+size_t orc_tree_query(const orc_node* nodes, size_t count, const float ray[6], int stop,
+                      uint32_t* hits, size_t max_hits, int* missed);
+
 /* Threads this process would use by default (online CPUs). */
 int orc_default_threads(void);
 

@@ -76,6 +76,8 @@ def lib():
         L.orc_disk.argtypes = [_F, _SZ, _F]
         L.orc_cube.argtypes = [_F, _SZ, _F]
         L.orc_disk_positions.argtypes = [_F, _SZ, _F, _SZ, _SZ]
+        L.orc_tree_query.argtypes = [C.c_void_p, _SZ, _F, C.c_int, _U32, _SZ, C.POINTER(C.c_int)]
+        L.orc_tree_query.restype = _SZ
         _lib = L
     return _lib
 
@@ -107,6 +109,8 @@ def ref_lib():
         L.ref_disk.argtypes = [_F, _SZ, C.c_float, C.c_float, C.c_float, C.c_float]
         L.ref_cube.argtypes = [_F, _SZ]
         L.ref_disk_args.argtypes = [_F, _SZ, _SZ, _SZ, _F]
+        L.ref_tree_query.argtypes = [_F, _SZ, C.c_float, _F, C.c_int, _U32, _SZ]
+        L.ref_tree_query.restype = _SZ
         L.ref_cube_args.argtypes = [_F, _SZ, _SZ, _SZ, _F]
         _ref = L
     return _ref
@@ -198,6 +202,13 @@ class Tree:
         lib().orc_tree_accel(self._t, _p(b, _F), len(b), _p(t, _I64), 0 if t is None else len(t),
                              theta, G, _p(out, _F), _p(inter, _U64), nthreads)
         return out, int(inter[0])
+
+
+def tree_nodes(bodies, size):
+    """detail::build_tree (tree.h:14-29) restated: the node array of the reference tree."""
+    t = Tree(size)
+    t.build(bodies, size)
+    return t.nodes()
 
 
 def nodes_accel(nodes, bodies, theta, G, targets=None, nthreads=0):
@@ -376,3 +387,27 @@ def ref_cube_range(bodies: np.ndarray, begin: int, num: int, **kw) -> np.ndarray
     b = np.ascontiguousarray(bodies, np.float32).copy()
     ref_lib().ref_cube_args(_p(b, _F), len(b), begin, num, _p(cube_arg_array(**kw), _F))
     return b
+
+
+# --- ray query (source/bhtree.cpp:153-173) -------------------------------------------------
+
+def tree_query(nodes: np.ndarray, ray, stop: int = 0, max_hits: int = 1 << 16):
+    """Tree::query over a node array (NODE_DTYPE) for one ray: (visited indices, visited
+    count, whether the walk passed a node the ray misses)."""
+    nodes = np.ascontiguousarray(nodes)
+    r = np.ascontiguousarray(ray, np.float32)
+    hits = np.zeros(max_hits, np.uint32)
+    missed = C.c_int()
+    cnt = lib().orc_tree_query(nodes.ctypes.data_as(C.c_void_p), len(nodes), _p(r, _F), stop, _p(hits, _U32),
+                               max_hits, C.byref(missed))
+    return hits[:min(cnt, max_hits)], int(cnt), bool(missed.value)
+
+
+def ref_tree_query(bodies: np.ndarray, size: float, ray, stop: int = 0, max_hits: int = 1 << 16):
+    """The reference's Tree::query over detail::build_tree(bodies, size). Only for rays
+    that meet every node the walk reaches: elsewhere the reference's loop never ends."""
+    b = np.ascontiguousarray(bodies, np.float32)
+    r = np.ascontiguousarray(ray, np.float32)
+    hits = np.zeros(max_hits, np.uint32)
+    cnt = ref_lib().ref_tree_query(_p(b, _F), len(b), size, _p(r, _F), stop, _p(hits, _U32), max_hits)
+    return hits[:min(cnt, max_hits)], int(cnt)

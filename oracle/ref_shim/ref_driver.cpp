@@ -151,6 +151,30 @@ extern "C"
             std::memcpy(bodies, bs.data(), n * sizeof(nbody::Body));
     }
 
+    // Tree::query (bhtree.cpp:153-173) over the tree detail::build_tree makes of the bodies,
+    // recording the visited node indices; stop 1: the visitor returns false at the first
+    // leaf with mass. The reference's loop does not advance past a node the ray misses, so
+    // callers pass only rays that meet every node the walk reaches.
+    size_t ref_tree_query(const float* bodies, size_t n, float size, const float* ray, int stop, uint32_t* hits,
+                          size_t max_hits)
+    {
+        std::vector<nbody::Body> bs(n);
+        if (n)
+            std::memcpy(bs.data(), bodies, n * sizeof(nbody::Body));
+        nbody::bh::Tree tree;
+        nbody::detail::build_tree(tree, bs, size);
+        const nbody::bh::Node* base = tree.nodes().data();
+        size_t visited = 0;
+        const nbody::Ray r{ { ray[0], ray[1], ray[2] }, { ray[3], ray[4], ray[5] } };
+        tree.query(r, [&](const nbody::bh::Node& node) {
+            if (visited < max_hits)
+                hits[visited] = static_cast<uint32_t>(&node - base);
+            ++visited;
+            return !(stop == 1 && node.children == 0 && node.mass != 0);
+        });
+        return visited;
+    }
+
     // util::disk over bodies[begin, begin + num) of an n-body array, every DiskArgs field
     // given: center[3], vel[3], axis[3], inner, outer, thickness, central mass, star mass.
     void ref_disk_args(float* bodies, size_t n, size_t begin, size_t num, const float* a)

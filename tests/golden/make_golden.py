@@ -14,6 +14,9 @@ oracle/build_oracle.py) and records its inputs and outputs:
   and the node arrays the reference builds for them.
 * ``scenes.npz`` -- util::disk and util::cube (util.cpp:14-126) over body ranges of
   arrays with other bodies around them, for the argument sets in DISK_CASES / CUBE_CASES.
+* ``query_cases.npz`` -- Tree::query (bhtree.cpp:153-173) on small random trees and rays,
+  visiting every met node or stopping at the first body, with the nodes the reference
+  visits (only cases where its walk ends: see query_fixtures).
 
 Usage: ``python tests/golden/make_golden.py`` (needs the reference checkout; the
 fixtures are committed so the tests never need it).
@@ -59,7 +62,56 @@ def main() -> None:
         out[f"{name}_nodes"] = O.ref_insert_points(pts, (0, 0, 0), 100.0).view(np.uint8)
     np.savez_compressed(HERE / "bhtree_cases.npz", **out)
     np.savez_compressed(HERE / "scenes.npz", **scene_fixtures())
+    np.savez_compressed(HERE / "query_cases.npz", **query_fixtures())
     print("fixtures written to", HERE)
+
+
+def query_fixtures(per_stop: int = 40) -> dict:
+    """Tree::query (bhtree.cpp:153-173) on random small trees and rays. The reference's loop
+    never ends once the walk reaches a node the ray misses, so only cases whose walk (per
+    the oracle) meets every node it reaches are kept, and the reference runs them in a
+    child process with a time limit."""
+    import subprocess
+    import tempfile
+    rng = np.random.default_rng(77)
+    cases = []
+    counts = {0: 0, 1: 0}
+    while min(counts.values()) < per_stop:
+        n = int(rng.integers(1, 48))
+        b = np.zeros((n, 12), np.float32)
+        b[:, :3] = rng.normal(0, 20, (n, 3)).astype(np.float32)
+        b[:, 7] = rng.uniform(0.5, 2.0, n).astype(np.float32)
+        nodes = O.ref_build_tree(b, 100.0)
+        ray = np.r_[rng.normal(0, 30, 3), rng.normal(0, 1, 3)].astype(np.float32)
+        for stop in (0, 1):
+            if counts[stop] >= per_stop:
+                continue
+            _, _, missed = O.tree_query(nodes, ray, stop)
+            if not missed:
+                cases.append((b, ray, stop))
+                counts[stop] += 1
+    with tempfile.TemporaryDirectory() as tmp:
+        src = Path(tmp) / "cases.npz"
+        dst = Path(tmp) / "hits.npz"
+        np.savez(src, **{f"b{i}": c[0] for i, c in enumerate(cases)},
+                 rays=np.stack([c[1] for c in cases]), stops=np.array([c[2] for c in cases]))
+        script = (
+            "import sys, numpy as np; sys.path.insert(0, %r)\n"
+            "from oracle import oracle as O\n"
+            "z = np.load(%r); out = {}\n"
+            "for i, (r, s) in enumerate(zip(z['rays'], z['stops'])):\n"
+            "    h, c = O.ref_tree_query(z[f'b{i}'], 100.0, r, int(s))\n"
+            "    out[f'h{i}'] = h; out[f'c{i}'] = np.array([c])\n"
+            "np.savez(%r, **out)\n" % (str(HERE.parent.parent), str(src), str(dst)))
+        subprocess.run([sys.executable, "-c", script], check=True, timeout=120)
+        res = np.load(dst)
+        out = {"rays": np.stack([c[1] for c in cases]), "stops": np.array([c[2] for c in cases], np.int32),
+               "size": np.array([100.0], np.float32)}
+        for i, c in enumerate(cases):
+            out[f"bodies_{i}"] = c[0]
+            out[f"hits_{i}"] = res[f"h{i}"]
+            out[f"count_{i}"] = res[f"c{i}"]
+    return out
 
 
 # util::disk / util::cube argument sets: (total bodies, begin, num, keyword arguments)
