@@ -349,16 +349,16 @@ int nbody_cuda_direct_autotune(nbody_cuda* ctx, const nbody_step_params* p, doub
  * diagnostics. Upload the concatenated bodies first. */
 int nbody_cuda_set_systems(nbody_cuda* ctx, const int64_t* offsets, size_t nsys);
 
-/* Time every batched kernel configuration (threads per target, targets per thread, inner
- * unroll) on the current bodies and system table, keep the fastest for later batched steps
- * and return its index in *best; times_ms (optional, ntimes entries) receives each
+/* Time every batched kernel configuration (threads per CTA, targets per thread, sources
+ * per chunk) on the current bodies and system table, keep the fastest for later batched
+ * steps and return its index in *best; times_ms (optional, ntimes entries) receives each
  * configuration's accelerate time. Synchronous. */
 int nbody_cuda_batch_autotune(nbody_cuda* ctx, const nbody_step_params* p, double* times_ms,
                               size_t ntimes, int* best);
 /* Number of batched configurations; describe one (index < 0: the active one); pin one. */
 int nbody_cuda_batch_config_count(void);
-int nbody_cuda_batch_config(const nbody_cuda* ctx, int index, int* threads_per_target,
-                            int* targets_per_thread, int* unroll);
+int nbody_cuda_batch_config(const nbody_cuda* ctx, int index, int* threads_per_cta,
+                            int* targets_per_thread, int* sources_per_chunk);
 int nbody_cuda_batch_set_config(nbody_cuda* ctx, int index);
 
 /* FP64 diagnostics per system (one system covering every body when no table is set):

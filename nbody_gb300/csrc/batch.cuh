@@ -18,7 +18,7 @@ namespace nbg
     int batch_set_config(nbody_cuda* ctx, int index);
     int batch_get_config(const nbody_cuda* ctx);
     int batch_config_count();
-    void batch_config_describe(int index, int* tpt, int* t, int* unroll);
+    void batch_config_describe(int index, int* block, int* t, int* chunk);
     int batch_energy(nbody_cuda* ctx, const nbody_step_params* p, double* out);
     size_t batch_system_count(const nbody_cuda* ctx);
     void release_batch(nbody_cuda* ctx);

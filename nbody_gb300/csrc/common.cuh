@@ -62,6 +62,20 @@ namespace nbg
         return ok != 0;
     }
 
+    // As mbar_try_wait, but the thread may be suspended for up to hint_ns while the phase is
+    // incomplete instead of returning at once, so a waiting warp takes no issue slots from
+    // the warps that are computing.
+    __device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, const unsigned parity, const unsigned hint_ns)
+    {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity), "r"(hint_ns) : "memory");
+        return ok != 0;
+    }
+
     // Wait for phase `parity` of `bar` to complete, giving up after limit_ns.
     // Returns false on timeout (and records it in *err).
     __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, const unsigned parity,
@@ -72,7 +86,7 @@ namespace nbg
         const uint64_t start = globaltimer();
         for (;;)
         {
-            if (mbar_try_wait(bar, parity))
+            if (mbar_try_wait_suspend(bar, parity, 20000u))
                 return true;
             if (globaltimer() - start > limit_ns)
             {

@@ -341,7 +341,7 @@ class Context:
     def batch_config(self, index: int = -1) -> dict:
         v = [C.c_int() for _ in range(3)]
         self.check(lib().nbody_cuda_batch_config(self.h, index, *[C.byref(x) for x in v]))
-        return dict(zip(("threads_per_target", "targets_per_thread", "unroll"), (x.value for x in v)))
+        return dict(zip(("threads_per_cta", "targets_per_thread", "sources_per_chunk"), (x.value for x in v)))
 
     def batch_set_config(self, index: int):
         self.check(lib().nbody_cuda_batch_set_config(self.h, index))

@@ -24,7 +24,8 @@ def main(argv=None) -> int:
     ap.add_argument("--n", type=int, default=1 << 18)
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--theta", type=float, default=0.5)
-    ap.add_argument("--variant", type=int, default=-1, help="pin a direct-sum kernel shape")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="pin a direct-sum kernel shape (batched: the batched configuration)")
     a = ap.parse_args(argv)
 
     layout = native.LAYOUT_AOS if a.case == "direct-aos" else native.LAYOUT_SOA
@@ -35,7 +36,7 @@ def main(argv=None) -> int:
         with native.Context() as ctx:
             ctx.upload_bodies(bodies)
             ctx.set_systems(off)
-            ctx.batch_set_config(15)
+            ctx.batch_set_config(a.variant if a.variant >= 0 else 0)
             ctx.update(p, a.steps)
             ctx.synchronize()
             print(f"batched: bodies={len(bodies)} steps={a.steps} launches={ctx.launches()}")
