@@ -64,6 +64,10 @@ WORKLOAD = ("direct-sum step, N=1048576 uniform unit cube at rest, log-normal(0,
             "summing to 1, softened eps=1e-3, G=1, dt=1e-3, FP32, semi-implicit Euler")
 FLOP_PER_PAIR = 20
 N_SAMPLE = 65536
+# ncu DRAM bytes (read + write) of one N = 2^20 direct-sum launch, by (targets per thread,
+# block, jsplit): the j-split partials stay mostly in L2, so traffic is far below the
+# 16 MB x (1 + jsplit) the launch touches.
+MEASURED_TRAFFIC = {(4, 256, 4): 17975296 + 11777024}
 
 
 def env_rank():
@@ -314,8 +318,11 @@ def _bench_gpu(args, stream):
                                         "MEASURED_PEAKS.json carries no FP32 figure",
                          "peak_scalar_ffma": s_tf, "peak_packed_ffma2": p_tf,
                          "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs,
-                         "kernel_ms": acc_ms, "traffic": 139991040,
-                         "traffic_note": "dram bytes read+write of one N=2^20 launch, ncu (profiles/direct_fp32_n262144_full.md)"},
+                         "kernel_ms": acc_ms,
+                         "traffic": MEASURED_TRAFFIC.get((cfg["targets_per_thread"], cfg["block"], cfg["jsplit"])),
+                         "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one N=2^20 launch of the "
+                                         "chosen shape (profiles/direct_fp32_n262144_full.md); null for a shape "
+                                         "not captured"},
             "cpu_baseline": {"value": cpu_rate / N, "unit": "body-steps/s", "cores": cores, "kind": kind,
                              "sample": sample + "; body-steps/s = pairs/s / N", "pairs_per_s": cpu_rate},
             "clocks": clocks.summary(),

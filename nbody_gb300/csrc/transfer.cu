@@ -18,6 +18,9 @@
 #include <thread>
 #include <vector>
 
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include "common.cuh"
 #include "context.cuh"
 
@@ -194,6 +197,24 @@ namespace nbg
             return (ctx->pageable_access && ctx->pageable_host_tables) ? NBODY_TRANSFER_DIRECT : NBODY_TRANSFER_MAPPED;
         }
 
+        // Whether every page of [p, p + bytes) is resident. The device writing pages that
+        // were never touched has each one faulted in and zeroed on its behalf, far slower
+        // than the CPU doing the same while it copies (800 MB: 198 ms against 13 ms on the
+        // test box), so a DIRECT download into such memory takes the MAPPED path instead.
+        bool pages_resident(const void* p, const size_t bytes)
+        {
+            static const size_t page = static_cast<size_t>(sysconf(_SC_PAGESIZE));
+            const uintptr_t lo = reinterpret_cast<uintptr_t>(p) & ~(page - 1);
+            const uintptr_t hi = reinterpret_cast<uintptr_t>(p) + bytes;
+            std::vector<unsigned char> vec((hi - lo + page - 1) / page);
+            if (mincore(reinterpret_cast<void*>(lo), hi - lo, vec.data()) != 0)
+                return true;    // not a mapping mincore can describe: let the device try
+            for (const unsigned char v : vec)
+                if (!(v & 1))
+                    return false;
+            return true;
+        }
+
         // The device address a kernel may use for host memory `p`: page-locked memory's
         // mapped address, or `p` itself when the device reaches pageable memory; null when
         // neither, or when `p` is not 16-byte aligned (the caller's path is then MAPPED).
@@ -327,6 +348,22 @@ namespace nbg
 
     int download_records(nbody_cuda* ctx, void* bodies, const size_t take, const unsigned mask)
     {
+        // DIRECT first: one device pass straight into the caller's records beats a host copy
+        // out of staging, even one already holding the current bodies
+        const int path = resolve(ctx);
+        if (path == NBODY_TRANSFER_DIRECT)
+        {
+            void* view = device_view(ctx, bodies);
+            if (view && view == bodies && !pages_resident(bodies, take * kRecord))
+                view = nullptr;     // pageable memory not yet touched: stage it (see pages_resident)
+            if (view)
+            {
+                const cudaError_t e = launch_out(ctx, view, take, mask);
+                if (e != cudaSuccess)
+                    return ctx_cuda_fail(ctx, e, "record write launch");
+                return check_device_error(ctx);
+            }
+        }
         // a predicted readback that is still current and holds every field asked for
         if (ctx->readback_valid && ctx->readback_version == ctx->body_version && ctx->readback_count >= take
             && !(mask & ~ctx->readback_mask))
@@ -339,17 +376,6 @@ namespace nbg
             merge_records(static_cast<float*>(bodies), static_cast<const float*>(ctx->mapped), take, mask);
             ++ctx->readback_hits;
             return NBODY_OK;
-        }
-        const int path = resolve(ctx);
-        if (path == NBODY_TRANSFER_DIRECT)
-        {
-            if (void* view = device_view(ctx, bodies))
-            {
-                const cudaError_t e = launch_out(ctx, view, take, mask);
-                if (e != cudaSuccess)
-                    return ctx_cuda_fail(ctx, e, "record write launch");
-                return check_device_error(ctx);
-            }
         }
         if (path == NBODY_TRANSFER_MAPPED || path == NBODY_TRANSFER_DIRECT)
         {
