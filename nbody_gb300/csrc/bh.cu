@@ -30,6 +30,7 @@
 //      would, in a different order.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "bh.cuh"
@@ -557,6 +558,194 @@ namespace nbg
         }
     }
 
+    // Two targets per lane: the packed form of apply(). Both halves run the scalar
+    // operations of apply() in the same order (an FP32x2 operation is two correctly rounded
+    // FP32 operations), and a half whose target does not take the node gets s = 0, which
+    // adds exactly zero. Targets are held as negated positions (d = s + (-x)).
+    template <int LAW>
+    __device__ __forceinline__ void apply2(const float2 npx, const float2 npy, const float2 npz, const float2 lim,
+                                           const float sx, const float sy, const float sz, const float m,
+                                           const bool take_a, const bool take_b, float2& ax, float2& ay, float2& az)
+    {
+        const float2 dx = add2(f2(sx), npx), dy = add2(f2(sy), npy), dz = add2(f2(sz), npz);
+        float2 r2 = (LAW == NBODY_LAW_SOFTENED) ? fma2(dx, dx, lim) : mul2(dx, dx);
+        r2 = fma2(dy, dy, r2);
+        r2 = fma2(dz, dz, r2);
+        float2 inv = make_float2(rsqrt_sfu(r2.x), rsqrt_sfu(r2.y));
+        if (LAW == NBODY_LAW_CUTOFF)
+        {
+            inv.x = r2.x > lim.x ? inv.x : 0.f;     // physics.h:38-39
+            inv.y = r2.y > lim.y ? inv.y : 0.f;
+        }
+        float2 sc = mul2(mul2(mul2(f2(m), inv), inv), inv);
+        sc.x = take_a ? sc.x : 0.f;
+        sc.y = take_b ? sc.y : 0.f;
+        ax = fma2(dx, sc, ax);
+        ay = fma2(dy, sc, ay);
+        az = fma2(dz, sc, az);
+    }
+
+    // The walk of traverse_kernel for 64 Morton-consecutive targets per warp: lane l holds
+    // targets 64 t + l (half a) and 64 t + 32 + l (half b), and a stack entry carries one lane
+    // mask per half. Each target still decides every node itself with the reference test,
+    // and its accepted nodes come in the same depth-first order, so its sum is the one
+    // traverse_kernel forms; one walk now serves twice the targets and every interaction is
+    // a packed pair.
+    template <int LAW>
+    __global__ void __launch_bounds__(kTravWarps * 32, 3) traverse2_kernel(
+        const OctNode* __restrict__ nodes, const float4* __restrict__ spm, const float* __restrict__ srad,
+        const uint32_t* __restrict__ order, const int n, const float G, const float eps2,
+        float4* __restrict__ acc, float* __restrict__ body_out, unsigned* __restrict__ err,
+        unsigned long long* __restrict__ stats)
+    {
+        // {cell index, lanes of half a that opened it, lanes of half b, unused}
+        __shared__ int4 stk[kTravWarps][kStack];
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const unsigned lt = (1u << lane) - 1u;
+        unsigned inter = 0, visits = 0;
+
+        for (int tile = blockIdx.x * kTravWarps + warp; tile * 64 < n; tile += gridDim.x * kTravWarps)
+        {
+            const int ka = tile * 64 + lane, kb = ka + 32;
+            const bool va = ka < n, vb = kb < n;
+            const float4 pa = spm[va ? ka : n - 1], pb = spm[vb ? kb : n - 1];
+            float2 lim;
+            if (LAW == NBODY_LAW_CUTOFF)
+            {
+                const float ra = srad[va ? ka : n - 1], rb = srad[vb ? kb : n - 1];
+                lim = make_float2(ra * ra, rb * rb);
+            }
+            else
+                lim = make_float2(eps2, eps2);
+            const float2 npx = make_float2(-pa.x, -pb.x), npy = make_float2(-pa.y, -pb.y);
+            const float2 npz = make_float2(-pa.z, -pb.z);
+            float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
+            const unsigned ma0 = __ballot_sync(0xffffffffu, va), mb0 = __ballot_sync(0xffffffffu, vb);
+            if (lane == 0)
+                stk[warp][0] = make_int4(0, static_cast<int>(ma0), static_cast<int>(mb0), 0);
+            int sp = 1;
+            __syncwarp();
+            // Each cell is reached from its one parent, so a warp pops at most one entry
+            // per cell (< n). The bound only trips on a malformed tree: it records the
+            // error and stops this warp instead of spinning.
+            int guard = 0;
+            const int guard_limit = n + 64;
+            while (sp > 0)
+            {
+                if (++guard > guard_limit)
+                {
+                    if (lane == 0)
+                        atomicOr(err, DEV_ERR_BOUNDS);
+                    break;
+                }
+                --sp;
+                const int4 top = stk[warp][sp];
+                __syncwarp();
+                const int nd = top.x;
+                const unsigned mask_a = static_cast<unsigned>(top.y), mask_b = static_cast<unsigned>(top.z);
+                ++visits;
+                const OctNode* cell = nodes + nd;
+                const float4 cm = cell->com_mass;
+                const int4 meta = *reinterpret_cast<const int4*>(&cell->open_r2);
+                const int cslot = cell->child[lane & 7];
+                if (cm.w == 0.f)
+                    continue;       // bhtree.cpp:109-113: empty nodes are skipped
+                // bhtree.cpp:117-125, evaluated in the reference's operation order, per target,
+                // with scalar operations the compiler may not fuse: a packed multiply-add chain
+                // can be contracted, and one rounding less flips borderline acceptances
+                const float2 dx = add2(f2(cm.x), npx), dy = add2(f2(cm.y), npy), dz = add2(f2(cm.z), npz);
+                const float ds_a = __fadd_rn(__fadd_rn(__fmul_rn(dx.x, dx.x), __fmul_rn(dy.x, dy.x)), __fmul_rn(dz.x, dz.x));
+                const float ds_b = __fadd_rn(__fadd_rn(__fmul_rn(dx.y, dx.y), __fmul_rn(dy.y, dy.y)), __fmul_rn(dz.y, dz.y));
+                const float open_r2 = __int_as_float(meta.x);
+                const bool acc_a = ((mask_a >> lane) & 1u) && ds_a > open_r2;
+                const bool acc_b = ((mask_b >> lane) & 1u) && ds_b > open_r2;
+                if (acc_a || acc_b)
+                {
+                    apply2<LAW>(npx, npy, npz, lim, cm.x, cm.y, cm.z, cm.w, acc_a, acc_b, ax, ay, az);
+                    inter += static_cast<unsigned>(acc_a) + static_cast<unsigned>(acc_b);
+                }
+                const unsigned open_a = mask_a & ~__ballot_sync(0xffffffffu, acc_a);
+                const unsigned open_b = mask_b & ~__ballot_sync(0xffffffffu, acc_b);
+                if (!(open_a | open_b))
+                    continue;
+                const bool mine_a = (open_a >> lane) & 1u, mine_b = (open_b >> lane) & 1u;
+                const int nchild = meta.y;
+                if (nchild < 0)
+                {
+                    for (int q = meta.z; q <= meta.w; ++q)
+                    {
+                        const float4 sb = spm[q];
+                        if (mine_a || mine_b)
+                        {
+                            apply2<LAW>(npx, npy, npz, lim, sb.x, sb.y, sb.z, sb.w, mine_a, mine_b, ax, ay, az);
+                            inter += static_cast<unsigned>(mine_a) + static_cast<unsigned>(mine_b);
+                        }
+                    }
+                    continue;
+                }
+                const int c = lane < nchild ? cslot : 0;
+                const bool is_cell = lane < nchild && c >= 0;
+                const bool is_leaf = lane < nchild && c < 0;
+                // each child lane fetches its own leaf body, so the leaf loop below only
+                // broadcasts registers
+                const float4 leaf = is_leaf ? spm[~c] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const unsigned cells = __ballot_sync(0xffffffffu, is_cell);
+                unsigned leaves = __ballot_sync(0xffffffffu, is_leaf && leaf.w != 0.f);
+                if (is_cell)
+                {
+                    const int at = sp + __popc(cells & lt);
+                    if (at < kStack)
+                        stk[warp][at] = make_int4(c, static_cast<int>(open_a), static_cast<int>(open_b), 0);
+                    else
+                        atomicOr(err, DEV_ERR_BOUNDS);
+                }
+                sp = min(kStack, sp + __popc(cells));
+                __syncwarp();
+                while (leaves)
+                {
+                    const int l = __ffs(leaves) - 1;
+                    leaves &= leaves - 1;
+                    const float sx = __shfl_sync(0xffffffffu, leaf.x, l);
+                    const float sy = __shfl_sync(0xffffffffu, leaf.y, l);
+                    const float sz = __shfl_sync(0xffffffffu, leaf.z, l);
+                    const float sw = __shfl_sync(0xffffffffu, leaf.w, l);
+                    if (mine_a || mine_b)
+                    {
+                        apply2<LAW>(npx, npy, npz, lim, sx, sy, sz, sw, mine_a, mine_b, ax, ay, az);
+                        inter += static_cast<unsigned>(mine_a) + static_cast<unsigned>(mine_b);
+                    }
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+            {
+                const int k = h ? kb : ka;
+                if (!(h ? vb : va))
+                    continue;
+                const uint32_t i = order[k];
+                const float gx = G * (h ? ax.y : ax.x), gy = G * (h ? ay.y : ay.x), gz = G * (h ? az.y : az.x);
+                if (body_out)
+                {
+                    float* o = body_out + static_cast<size_t>(i) * 12 + 8;
+                    o[0] = gx;
+                    o[1] = gy;
+                    o[2] = gz;
+                }
+                else
+                    acc[i] = make_float4(gx, gy, gz, 0.f);
+            }
+        }
+        // per-warp totals
+        unsigned long long total = inter;
+        for (int o = 16; o > 0; o >>= 1)
+            total += __shfl_down_sync(0xffffffffu, total, o);
+        if (lane == 0)
+        {
+            atomicAdd(&stats[0], total);
+            atomicAdd(&stats[1], static_cast<unsigned long long>(visits));
+        }
+    }
+
     // ------------------------------------------------------------------------------------
     // host side
     // ------------------------------------------------------------------------------------
@@ -727,6 +916,25 @@ namespace nbg
         }
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        // 64 targets per warp (traverse2_kernel) unless NBODY_CUDA_BH_TARGETS=32 asks for the
+        // one-target-per-lane walk; both give the same sums
+        const char* tsel = std::getenv("NBODY_CUDA_BH_TARGETS");
+        if (!(tsel && std::strcmp(tsel, "32") == 0))
+        {
+            // one resident wave of CTAs: the grid-stride loop gives every CTA the same number
+            // of tiles, so a second, partial wave would leave most SMs idle
+            auto fn = p->law == NBODY_LAW_SOFTENED ? traverse2_kernel<NBODY_LAW_SOFTENED> : traverse2_kernel<NBODY_LAW_CUTOFF>;
+            int per = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kTravWarps * 32, 0) != cudaSuccess || per < 1)
+                per = 1;
+            const int tiles2 = (ni + 63) / 64;
+            const int grid2 = std::min((tiles2 + kTravWarps - 1) / kTravWarps, sms * per);
+            fn<<<grid2, kTravWarps * 32, 0, s>>>(b.nodes, b.spm, b.srad, b.order, ni, p->G, p->eps2, acc, body_out,
+                                                  ctx->dev_error, b.stats);
+            ++ctx->launches;
+            const cudaError_t e2 = cudaGetLastError();
+            return e2 == cudaSuccess ? NBODY_OK : ctx_cuda_fail(ctx, e2, "tree traversal");
+        }
         const int tiles = (ni + 31) / 32;
         const int grid = std::min((tiles + kTravWarps - 1) / kTravWarps, sms * 8);
         if (p->law == NBODY_LAW_SOFTENED)
