@@ -585,44 +585,66 @@ namespace nbg
         az = fma2(dz, sc, az);
     }
 
-    // The walk of traverse_kernel for 64 Morton-consecutive targets per warp: lane l holds
-    // targets 64 t + l (half a) and 64 t + 32 + l (half b), and a stack entry carries one lane
-    // mask per half. Each target still decides every node itself with the reference test,
-    // and its accepted nodes come in the same depth-first order, so its sum is the one
-    // traverse_kernel forms; one walk now serves twice the targets and every interaction is
-    // a packed pair.
-    template <int LAW>
-    __global__ void __launch_bounds__(kTravWarps * 32, 3) traverse2_kernel(
+    // The walk of traverse_kernel for 64 Q Morton-consecutive targets per warp: lane l holds
+    // targets 64 Q t + 32 h + l for h < 2Q, as Q packed pairs (halves 2p and 2p + 1), and a
+    // stack entry carries one lane mask per target slot h. Each target still decides every
+    // node itself with the reference test, and its accepted nodes come in the same
+    // depth-first order, so its sum is the one traverse_kernel forms; one walk now serves
+    // 2Q times the targets and every interaction is a packed pair.
+    template <int LAW, int Q>
+    __global__ void __launch_bounds__(kTravWarps * 32, 2) traverse_pairs_kernel(
         const OctNode* __restrict__ nodes, const float4* __restrict__ spm, const float* __restrict__ srad,
         const uint32_t* __restrict__ order, const int n, const float G, const float eps2,
         float4* __restrict__ acc, float* __restrict__ body_out, unsigned* __restrict__ err,
         unsigned long long* __restrict__ stats)
     {
-        // {cell index, lanes of half a that opened it, lanes of half b, unused}
-        __shared__ int4 stk[kTravWarps][kStack];
+        constexpr int H = 2 * Q;                    // target slots per lane
+        constexpr int TW = 32 * H;                  // targets per warp walk
+        __shared__ int stk_cell[kTravWarps][kStack];
+        __shared__ unsigned stk_mask[kTravWarps][kStack][H];    // lanes of each slot that opened it
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         const unsigned lt = (1u << lane) - 1u;
         unsigned inter = 0, visits = 0;
 
-        for (int tile = blockIdx.x * kTravWarps + warp; tile * 64 < n; tile += gridDim.x * kTravWarps)
+        for (int tile = blockIdx.x * kTravWarps + warp; tile * TW < n; tile += gridDim.x * kTravWarps)
         {
-            const int ka = tile * 64 + lane, kb = ka + 32;
-            const bool va = ka < n, vb = kb < n;
-            const float4 pa = spm[va ? ka : n - 1], pb = spm[vb ? kb : n - 1];
-            float2 lim;
-            if (LAW == NBODY_LAW_CUTOFF)
+            float2 npx[Q], npy[Q], npz[Q], lim[Q], ax[Q], ay[Q], az[Q];
+            unsigned m0[H];
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
             {
-                const float ra = srad[va ? ka : n - 1], rb = srad[vb ? kb : n - 1];
-                lim = make_float2(ra * ra, rb * rb);
+                float v[2][4];
+#pragma unroll
+                for (int e = 0; e < 2; ++e)
+                {
+                    const int k = tile * TW + (2 * q + e) * 32 + lane;
+                    const bool valid = k < n;
+                    m0[2 * q + e] = __ballot_sync(0xffffffffu, valid);
+                    const float4 pk = spm[valid ? k : n - 1];
+                    v[e][0] = -pk.x;
+                    v[e][1] = -pk.y;
+                    v[e][2] = -pk.z;
+                    if (LAW == NBODY_LAW_CUTOFF)
+                    {
+                        const float r = srad[valid ? k : n - 1];
+                        v[e][3] = r * r;
+                    }
+                    else
+                        v[e][3] = eps2;
+                }
+                npx[q] = make_float2(v[0][0], v[1][0]);
+                npy[q] = make_float2(v[0][1], v[1][1]);
+                npz[q] = make_float2(v[0][2], v[1][2]);
+                lim[q] = make_float2(v[0][3], v[1][3]);
+                ax[q] = ay[q] = az[q] = make_float2(0.f, 0.f);
             }
-            else
-                lim = make_float2(eps2, eps2);
-            const float2 npx = make_float2(-pa.x, -pb.x), npy = make_float2(-pa.y, -pb.y);
-            const float2 npz = make_float2(-pa.z, -pb.z);
-            float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
-            const unsigned ma0 = __ballot_sync(0xffffffffu, va), mb0 = __ballot_sync(0xffffffffu, vb);
             if (lane == 0)
-                stk[warp][0] = make_int4(0, static_cast<int>(ma0), static_cast<int>(mb0), 0);
+            {
+                stk_cell[warp][0] = 0;
+#pragma unroll
+                for (int h = 0; h < H; ++h)
+                    stk_mask[warp][0][h] = m0[h];
+            }
             int sp = 1;
             __syncwarp();
             // Each cell is reached from its one parent, so a warp pops at most one entry
@@ -639,10 +661,12 @@ namespace nbg
                     break;
                 }
                 --sp;
-                const int4 top = stk[warp][sp];
+                const int nd = stk_cell[warp][sp];
+                unsigned mask[H];
+#pragma unroll
+                for (int h = 0; h < H; ++h)
+                    mask[h] = stk_mask[warp][sp][h];
                 __syncwarp();
-                const int nd = top.x;
-                const unsigned mask_a = static_cast<unsigned>(top.y), mask_b = static_cast<unsigned>(top.z);
                 ++visits;
                 const OctNode* cell = nodes + nd;
                 const float4 cm = cell->com_mass;
@@ -650,35 +674,63 @@ namespace nbg
                 const int cslot = cell->child[lane & 7];
                 if (cm.w == 0.f)
                     continue;       // bhtree.cpp:109-113: empty nodes are skipped
-                // bhtree.cpp:117-125, evaluated in the reference's operation order, per target,
-                // with scalar operations the compiler may not fuse: a packed multiply-add chain
-                // can be contracted, and one rounding less flips borderline acceptances
-                const float2 dx = add2(f2(cm.x), npx), dy = add2(f2(cm.y), npy), dz = add2(f2(cm.z), npz);
-                const float ds_a = __fadd_rn(__fadd_rn(__fmul_rn(dx.x, dx.x), __fmul_rn(dy.x, dy.x)), __fmul_rn(dz.x, dz.x));
-                const float ds_b = __fadd_rn(__fadd_rn(__fmul_rn(dx.y, dx.y), __fmul_rn(dy.y, dy.y)), __fmul_rn(dz.y, dz.y));
                 const float open_r2 = __int_as_float(meta.x);
-                const bool acc_a = ((mask_a >> lane) & 1u) && ds_a > open_r2;
-                const bool acc_b = ((mask_b >> lane) & 1u) && ds_b > open_r2;
-                if (acc_a || acc_b)
+                bool take[H];
+                bool any_take = false;
+                unsigned open_any = 0;
+                unsigned open[H];
+#pragma unroll
+                for (int q = 0; q < Q; ++q)
                 {
-                    apply2<LAW>(npx, npy, npz, lim, cm.x, cm.y, cm.z, cm.w, acc_a, acc_b, ax, ay, az);
-                    inter += static_cast<unsigned>(acc_a) + static_cast<unsigned>(acc_b);
+                    // bhtree.cpp:117-125, evaluated in the reference's operation order, per
+                    // target, with scalar operations the compiler may not fuse: a packed
+                    // multiply-add chain can be contracted, and one rounding less flips
+                    // borderline acceptances
+                    const float2 dx = add2(f2(cm.x), npx[q]), dy = add2(f2(cm.y), npy[q]), dz = add2(f2(cm.z), npz[q]);
+                    const float ds0 = __fadd_rn(__fadd_rn(__fmul_rn(dx.x, dx.x), __fmul_rn(dy.x, dy.x)), __fmul_rn(dz.x, dz.x));
+                    const float ds1 = __fadd_rn(__fadd_rn(__fmul_rn(dx.y, dx.y), __fmul_rn(dy.y, dy.y)), __fmul_rn(dz.y, dz.y));
+                    take[2 * q] = ((mask[2 * q] >> lane) & 1u) && ds0 > open_r2;
+                    take[2 * q + 1] = ((mask[2 * q + 1] >> lane) & 1u) && ds1 > open_r2;
+                    if (take[2 * q] || take[2 * q + 1])
+                    {
+                        apply2<LAW>(npx[q], npy[q], npz[q], lim[q], cm.x, cm.y, cm.z, cm.w, take[2 * q],
+                                    take[2 * q + 1], ax[q], ay[q], az[q]);
+                        inter += static_cast<unsigned>(take[2 * q]) + static_cast<unsigned>(take[2 * q + 1]);
+                    }
                 }
-                const unsigned open_a = mask_a & ~__ballot_sync(0xffffffffu, acc_a);
-                const unsigned open_b = mask_b & ~__ballot_sync(0xffffffffu, acc_b);
-                if (!(open_a | open_b))
+#pragma unroll
+                for (int h = 0; h < H; ++h)
+                {
+                    open[h] = mask[h] & ~__ballot_sync(0xffffffffu, take[h]);
+                    open_any |= open[h];
+                    any_take |= take[h];
+                }
+                (void)any_take;
+                if (!open_any)
                     continue;
-                const bool mine_a = (open_a >> lane) & 1u, mine_b = (open_b >> lane) & 1u;
+                bool mine[H], mine_any = false;
+#pragma unroll
+                for (int h = 0; h < H; ++h)
+                {
+                    mine[h] = (open[h] >> lane) & 1u;
+                    mine_any |= mine[h];
+                }
                 const int nchild = meta.y;
                 if (nchild < 0)
                 {
-                    for (int q = meta.z; q <= meta.w; ++q)
+                    for (int b = meta.z; b <= meta.w; ++b)
                     {
-                        const float4 sb = spm[q];
-                        if (mine_a || mine_b)
+                        const float4 sb = spm[b];
+                        if (mine_any)
                         {
-                            apply2<LAW>(npx, npy, npz, lim, sb.x, sb.y, sb.z, sb.w, mine_a, mine_b, ax, ay, az);
-                            inter += static_cast<unsigned>(mine_a) + static_cast<unsigned>(mine_b);
+#pragma unroll
+                            for (int q = 0; q < Q; ++q)
+                                if (mine[2 * q] || mine[2 * q + 1])
+                                {
+                                    apply2<LAW>(npx[q], npy[q], npz[q], lim[q], sb.x, sb.y, sb.z, sb.w, mine[2 * q],
+                                                mine[2 * q + 1], ax[q], ay[q], az[q]);
+                                    inter += static_cast<unsigned>(mine[2 * q]) + static_cast<unsigned>(mine[2 * q + 1]);
+                                }
                         }
                     }
                     continue;
@@ -695,7 +747,12 @@ namespace nbg
                 {
                     const int at = sp + __popc(cells & lt);
                     if (at < kStack)
-                        stk[warp][at] = make_int4(c, static_cast<int>(open_a), static_cast<int>(open_b), 0);
+                    {
+                        stk_cell[warp][at] = c;
+#pragma unroll
+                        for (int h = 0; h < H; ++h)
+                            stk_mask[warp][at][h] = open[h];
+                    }
                     else
                         atomicOr(err, DEV_ERR_BOUNDS);
                 }
@@ -709,31 +766,40 @@ namespace nbg
                     const float sy = __shfl_sync(0xffffffffu, leaf.y, l);
                     const float sz = __shfl_sync(0xffffffffu, leaf.z, l);
                     const float sw = __shfl_sync(0xffffffffu, leaf.w, l);
-                    if (mine_a || mine_b)
+                    if (mine_any)
                     {
-                        apply2<LAW>(npx, npy, npz, lim, sx, sy, sz, sw, mine_a, mine_b, ax, ay, az);
-                        inter += static_cast<unsigned>(mine_a) + static_cast<unsigned>(mine_b);
+#pragma unroll
+                        for (int q = 0; q < Q; ++q)
+                            if (mine[2 * q] || mine[2 * q + 1])
+                            {
+                                apply2<LAW>(npx[q], npy[q], npz[q], lim[q], sx, sy, sz, sw, mine[2 * q], mine[2 * q + 1],
+                                            ax[q], ay[q], az[q]);
+                                inter += static_cast<unsigned>(mine[2 * q]) + static_cast<unsigned>(mine[2 * q + 1]);
+                            }
                     }
                 }
             }
 #pragma unroll
-            for (int h = 0; h < 2; ++h)
-            {
-                const int k = h ? kb : ka;
-                if (!(h ? vb : va))
-                    continue;
-                const uint32_t i = order[k];
-                const float gx = G * (h ? ax.y : ax.x), gy = G * (h ? ay.y : ay.x), gz = G * (h ? az.y : az.x);
-                if (body_out)
+            for (int q = 0; q < Q; ++q)
+#pragma unroll
+                for (int e = 0; e < 2; ++e)
                 {
-                    float* o = body_out + static_cast<size_t>(i) * 12 + 8;
-                    o[0] = gx;
-                    o[1] = gy;
-                    o[2] = gz;
+                    const int k = tile * TW + (2 * q + e) * 32 + lane;
+                    if (k >= n)
+                        continue;
+                    const uint32_t i = order[k];
+                    const float gx = G * (e ? ax[q].y : ax[q].x), gy = G * (e ? ay[q].y : ay[q].x);
+                    const float gz = G * (e ? az[q].y : az[q].x);
+                    if (body_out)
+                    {
+                        float* o = body_out + static_cast<size_t>(i) * 12 + 8;
+                        o[0] = gx;
+                        o[1] = gy;
+                        o[2] = gz;
+                    }
+                    else
+                        acc[i] = make_float4(gx, gy, gz, 0.f);
                 }
-                else
-                    acc[i] = make_float4(gx, gy, gz, 0.f);
-            }
         }
         // per-warp totals
         unsigned long long total = inter;
@@ -916,18 +982,21 @@ namespace nbg
         }
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-        // 64 targets per warp (traverse2_kernel) unless NBODY_CUDA_BH_TARGETS=32 asks for the
-        // one-target-per-lane walk; both give the same sums
+        // 64 or 128 targets per warp walk (traverse_pairs_kernel, 2 or 4 per lane) unless
+        // NBODY_CUDA_BH_TARGETS=32 asks for the one-target-per-lane walk; all give the same sums
         const char* tsel = std::getenv("NBODY_CUDA_BH_TARGETS");
-        if (!(tsel && std::strcmp(tsel, "32") == 0))
+        const int per_warp = tsel ? std::atoi(tsel) : 128;
+        if (per_warp == 64 || per_warp == 128)
         {
+            const bool soft = p->law == NBODY_LAW_SOFTENED;
+            auto fn = per_warp == 128 ? (soft ? traverse_pairs_kernel<NBODY_LAW_SOFTENED, 2> : traverse_pairs_kernel<NBODY_LAW_CUTOFF, 2>)
+                                      : (soft ? traverse_pairs_kernel<NBODY_LAW_SOFTENED, 1> : traverse_pairs_kernel<NBODY_LAW_CUTOFF, 1>);
             // one resident wave of CTAs: the grid-stride loop gives every CTA the same number
             // of tiles, so a second, partial wave would leave most SMs idle
-            auto fn = p->law == NBODY_LAW_SOFTENED ? traverse2_kernel<NBODY_LAW_SOFTENED> : traverse2_kernel<NBODY_LAW_CUTOFF>;
             int per = 0;
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kTravWarps * 32, 0) != cudaSuccess || per < 1)
                 per = 1;
-            const int tiles2 = (ni + 63) / 64;
+            const int tiles2 = (ni + per_warp - 1) / per_warp;
             const int grid2 = std::min((tiles2 + kTravWarps - 1) / kTravWarps, sms * per);
             fn<<<grid2, kTravWarps * 32, 0, s>>>(b.nodes, b.spm, b.srad, b.order, ni, p->G, p->eps2, acc, body_out,
                                                   ctx->dev_error, b.stats);

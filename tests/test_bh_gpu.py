@@ -257,16 +257,18 @@ def test_tree_export_is_the_reference_tree(gpu, fixture):
     assert np.median(err) <= 1e-5 and (err > TOL).sum() <= len(b) // 500 + 2
 
 
+@pytest.mark.parametrize("per_warp", ["128", "64"])
 @pytest.mark.parametrize("law", [0, 1], ids=["cutoff", "softened"])
 @pytest.mark.parametrize("n", [1000, 4097, 100000])
-def test_two_targets_per_lane_walk_is_bit_identical(gpu, n, law, monkeypatch):
-    """The 64-targets-per-warp walk (the default) and the 32-target walk accept the same
-    nodes per target in the same depth-first order, so every acceleration and the
+def test_two_targets_per_lane_walk_is_bit_identical(gpu, n, law, per_warp, monkeypatch):
+    """The walks with 4 (the default) and 2 targets per lane and the 32-target walk accept
+    the same nodes per target in the same depth-first order, so every acceleration and the
     interaction count agree bit for bit."""
     from nbody_gb300 import scenes
     b = scenes.two_plummer(n // 2 + 1)[:n]
     b[:, 3] = np.float32(1e-3)
     kw = dict(theta=0.6, law=law, eps2=1e-4 if law == 1 else 0.0, size=0.0, tree_box=1)
+    monkeypatch.setenv("NBODY_CUDA_BH_TARGETS", per_warp)
     a64, s64 = bh_accel(gpu, b, **kw)
     monkeypatch.setenv("NBODY_CUDA_BH_TARGETS", "32")
     a32, s32 = bh_accel(gpu, b, **kw)
