@@ -175,14 +175,40 @@ namespace nbg
                 e = exp2(ceil(log2(ext)));
             if (e <= ext)
                 e *= 2.0;       // keep the maximum strictly inside the top cell
-            for (int a = 0; a < 3; ++a)
+            // centre the cube on the bodies, then move its corner down onto the cell grid
+            // (a shift of less than one cell); double the edge if that would uncover the
+            // maximum
+            for (int pass = 0; pass < 2; ++pass)
             {
-                b.center[a] = isfinite(lo[a]) ? 0.5 * (lo[a] + hi[a]) : 0.0;
-                b.lo[a] = b.center[a] - 0.5 * e;
+                const double cell = e / static_cast<double>(1u << kMortonBits);
+                bool fits = true;
+                for (int a = 0; a < 3; ++a)
+                {
+                    const double c = isfinite(lo[a]) ? 0.5 * (lo[a] + hi[a]) : 0.0;
+                    b.lo[a] = floor((c - 0.5 * e) / cell) * cell;
+                    b.center[a] = b.lo[a] + 0.5 * e;
+                    fits = fits && (!isfinite(hi[a]) || hi[a] < b.lo[a] + e);
+                }
+                if (fits)
+                    break;
+                e *= 2.0;
             }
             b.edge = e;
         }
         b.inv_cell = static_cast<double>(1u << kMortonBits) / b.edge;
+        // the integer quantisation applies when the cells are powers of two and the corner
+        // sits on their grid (always for the fitted cube)
+        int ex = 0;
+        const double mant = frexp(b.edge, &ex);
+        b.cell_exp = ex - 1 - kMortonBits;
+        bool exact = mant == 0.5 && isfinite(b.edge) && b.cell_exp >= -149;
+        for (int a = 0; a < 3; ++a)
+        {
+            const double lc = ldexp(b.lo[a], -b.cell_exp);
+            exact = exact && lc == floor(lc) && fabs(lc) < 4.0e15;
+            b.lo_cells[a] = exact ? static_cast<long long>(lc) : 0;
+        }
+        b.exact = exact ? 1 : 0;
         *box = b;
     }
 
@@ -211,6 +237,41 @@ namespace nbg
         return static_cast<uint64_t>(f);
     }
 
+    // The same cell index with integer operations only, for a box whose cells are 2^cell_exp
+    // and whose corner is lo_cells cells from the origin: x = M 2^E exactly (M the 24-bit
+    // significand), so floor(x / cell) = floor(M 2^(E - cell_exp)) is a shift (rounding
+    // toward -inf for negative x), and the index is that minus lo_cells, clamped. It equals
+    // quantise() there: the directed roundings make floor(rd(rd(x - lo) * inv_cell)) the
+    // exact floor((x - lo) / cell) when every cell boundary is a double.
+    __device__ __forceinline__ uint64_t quantise_exact(const float x, const int cell_exp, const long long lo_cells)
+    {
+        const uint32_t bits = __float_as_uint(x);
+        const uint32_t e = (bits >> 23) & 0xffu;
+        const uint32_t frac = bits & 0x7fffffu;
+        const bool neg = bits >> 31;
+        if (e == 0xffu)
+            return (frac == 0 && !neg) ? 2097151u : 0u;     // +inf clamps high; -inf and NaN to 0
+        const long long m = e ? static_cast<long long>(frac | 0x800000u) : static_cast<long long>(frac);
+        const int s = (e ? static_cast<int>(e) - 150 : -149) - cell_exp;     // x / cell = m 2^s
+        long long cells;
+        if (s >= 0)
+        {
+            if (s > 38)     // |x| / cell >= 2^61: far outside the box
+                return neg ? 0u : 2097151u;
+            cells = neg ? -(m << s) : (m << s);
+        }
+        else
+        {
+            const int r = -s;
+            if (r >= 62)
+                cells = (neg && m) ? -1 : 0;
+            else
+                cells = neg ? -((m + (1ll << r) - 1) >> r) : (m >> r);
+        }
+        const long long q = cells - lo_cells;
+        return q < 0 ? 0u : (q > 2097151 ? 2097151u : static_cast<uint64_t>(q));
+    }
+
     __global__ void morton_kernel(const float4* __restrict__ src, const int stride, const int n,
                                   const BoxParams* __restrict__ box, uint64_t* __restrict__ keys,
                                   uint32_t* __restrict__ vals)
@@ -219,9 +280,21 @@ namespace nbg
         if (i >= n)
             return;
         const float4 p = src[static_cast<size_t>(i) * stride];
-        const BoxParams b = *box;
-        keys[i] = spread3(quantise(p.x, b.lo[0], b.inv_cell)) | (spread3(quantise(p.y, b.lo[1], b.inv_cell)) << 1)
-                  | (spread3(quantise(p.z, b.lo[2], b.inv_cell)) << 2);
+        const BoxParams& b = *box;
+        uint64_t qx, qy, qz;
+        if (b.exact)
+        {
+            qx = quantise_exact(p.x, b.cell_exp, b.lo_cells[0]);
+            qy = quantise_exact(p.y, b.cell_exp, b.lo_cells[1]);
+            qz = quantise_exact(p.z, b.cell_exp, b.lo_cells[2]);
+        }
+        else
+        {
+            qx = quantise(p.x, b.lo[0], b.inv_cell);
+            qy = quantise(p.y, b.lo[1], b.inv_cell);
+            qz = quantise(p.z, b.lo[2], b.inv_cell);
+        }
+        keys[i] = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
         vals[i] = static_cast<uint32_t>(i);
     }
 

@@ -18,6 +18,11 @@ namespace nbg
         double center[3];   // centre (prefix sums are taken relative to it)
         double edge;        // cube edge
         double inv_cell;    // 2^21 / edge
+        // When the edge is a power of two and the corner lies on the cell grid, the cell
+        // index of x is floor(x / 2^cell_exp) - lo_cells exactly, in integers (see morton).
+        int exact;
+        int cell_exp;               // log2(edge / 2^21)
+        long long lo_cells[3];      // lo / cell
     };
 
     // One octree cell: 64 bytes, read whole by a warp (a broadcast load per field).

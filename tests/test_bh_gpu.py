@@ -89,6 +89,35 @@ def test_morton_and_sort_order_bit_exact(gpu):
             assert np.array_equal(codes, ref_codes[ref_order])
 
 
+@pytest.mark.parametrize("size,tree_box", [(64.0, 0), (100.0, 0), (0.0, 1)],
+                         ids=["pow2-box-integer-path", "other-box-fp64-path", "fitted-box"])
+def test_morton_codes_at_special_values(gpu, size, tree_box):
+    """The integer quantisation (power-of-two cells on a cell-aligned corner) and the FP64
+    directed-rounding one agree with the oracle bit for bit on signed zeros, subnormals,
+    values on and next to cell boundaries, values far outside the box and infinities."""
+    rng = np.random.default_rng(5)
+    special = np.array([0.0, -0.0, 1e-45, -1e-45, 1e-39, -1e-39, 1e-30, -1e-30, 31.999998, 32.0, -32.0,
+                        -32.000004, 1e30, -1e30, np.inf, -np.inf, 2.0 ** -19, -2.0 ** -19,
+                        np.nextafter(np.float32(2.0 ** -15), np.float32(0))], np.float32)
+    n = 4096
+    b = np.zeros((n, 12), np.float32)
+    b[:, :3] = rng.uniform(-30, 30, (n, 3)).astype(np.float32)
+    b[:, 7] = 1.0
+    k = len(special)
+    b[:k, 0] = special
+    b[k:2 * k, 1] = special
+    b[2 * k:3 * k, 2] = special
+    if tree_box == 1:           # keep the fitted box finite: no infinities for the bounding box
+        b[:, :3] = np.where(np.isfinite(b[:, :3]) & (np.abs(b[:, :3]) < 1e20), b[:, :3], 7.0)
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        codes, order, box = ctx.morton(gpu.params(mode=gpu.MODE_NLOGN, size=size, tree_box=tree_box))
+    ref_codes = O.morton63(b[:, :3], box[:3], 2.0 ** 21 / box[3])
+    ref_order = O.sort_order(ref_codes)
+    assert np.array_equal(order, ref_order)
+    assert np.array_equal(codes, ref_codes[ref_order])
+
+
 def test_morton_cells_are_reference_cells(gpu):
     """Every body's level-L Morton digit is its reference octant (bits flipped) in the
     reference's own tree (golden node array of the 4096-body cube)."""
