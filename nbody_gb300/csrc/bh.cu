@@ -403,6 +403,34 @@ namespace nbg
     // ------------------------------------------------------------------------------------
     // 6. octree records
     // ------------------------------------------------------------------------------------
+    // The children of a cell: walking down through the binary nodes of the cell's own level
+    // (at most three splits below it), every leaf body and every node of a deeper level is
+    // one child. Right subtrees first, which is the order the traversal has always used.
+    template <int DEPTH>
+    __device__ __forceinline__ void collect_children(const int c, const int2* __restrict__ child,
+                                                     const uint32_t* __restrict__ flag,
+                                                     const uint32_t* __restrict__ octidx, int* __restrict__ out,
+                                                     int& nc, unsigned* __restrict__ err)
+    {
+        if (c < 0 || flag[c])
+        {
+            if (nc < 8)
+                out[nc] = c < 0 ? c : static_cast<int>(octidx[c]);
+            else
+                atomicOr(err, DEV_ERR_BOUNDS);
+            ++nc;
+            return;
+        }
+        if (DEPTH == 0)
+        {
+            atomicOr(err, DEV_ERR_BOUNDS);      // more than three splits inside one octal level
+            return;
+        }
+        const int2 ch = child[c];
+        collect_children<DEPTH ? DEPTH - 1 : 0>(ch.y, child, flag, octidx, out, nc, err);
+        collect_children<DEPTH ? DEPTH - 1 : 0>(ch.x, child, flag, octidx, out, nc, err);
+    }
+
     __global__ void octnode_kernel(const int2* __restrict__ child, const int2* __restrict__ range,
                                    const int* __restrict__ prefix, const uint32_t* __restrict__ flag,
                                    const uint32_t* __restrict__ octidx, const double4* __restrict__ psum,
@@ -411,64 +439,43 @@ namespace nbg
                                    unsigned long long* __restrict__ stats)
     {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i == 0)
+            atomicAdd(&stats[2], static_cast<unsigned long long>(octidx[m - 1] + flag[m - 1]));
         if (i >= m || !flag[i])
             return;
         const int2 rg = range[i];
-        const int lvl = level_of(prefix[i]);
+        const int pre = prefix[i];
+        const int lvl = level_of(pre);
         const double4 hi = psum[rg.y + 1], lo = psum[rg.x];
         const double ms = hi.w - lo.w;
-        OctNode nd;
-        const BoxParams b = *box;
+        OctNode* out = nodes + octidx[i];
         if (ms > 0.0)
         {
-            nd.com_mass = make_float4(static_cast<float>(b.center[0] + (hi.x - lo.x) / ms),
-                                      static_cast<float>(b.center[1] + (hi.y - lo.y) / ms),
-                                      static_cast<float>(b.center[2] + (hi.z - lo.z) / ms), static_cast<float>(ms));
+            const double inv = 1.0 / ms;
+            out->com_mass = make_float4(static_cast<float>(box->center[0] + (hi.x - lo.x) * inv),
+                                        static_cast<float>(box->center[1] + (hi.y - lo.y) * inv),
+                                        static_cast<float>(box->center[2] + (hi.z - lo.z) * inv),
+                                        static_cast<float>(ms));
         }
         else
-            nd.com_mass = make_float4(0.f, 0.f, 0.f, 0.f);
+            out->com_mass = make_float4(0.f, 0.f, 0.f, 0.f);
         // the reference's node size is the root size halved per level, in float
-        const float s = static_cast<float>(ldexp(b.edge, -lvl));
-        const float size_sq = __fmul_rn(s, s);
-        nd.open_r2 = __fmul_rn(size_sq, __fmul_rn(theta, theta));
-        nd.first = rg.x;
-        nd.last = rg.y;
-        for (int c = 0; c < 8; ++c)
-            nd.child[c] = 0;
-        if (prefix[i] >= 3 * kMaxLevel)
-            nd.nchild = -1;     // bucket: identical codes, bodies applied one by one
+        const float sz = static_cast<float>(ldexp(box->edge, -lvl));
+        const float open_r2 = __fmul_rn(__fmul_rn(sz, sz), __fmul_rn(theta, theta));
+        int4* kids = reinterpret_cast<int4*>(out->child);
+        kids[0] = make_int4(0, 0, 0, 0);
+        kids[1] = make_int4(0, 0, 0, 0);
+        int nc = 0;
+        if (pre >= 3 * kMaxLevel)
+            nc = -1;     // bucket: identical codes, bodies applied one by one
         else
         {
-            // Walk down through the binary nodes of the same level (at most 7 below a cell
-            // with 8 children) collecting the next cells and single bodies.
-            int stack[8];
-            int sp = 0, nc = 0;
-            stack[sp++] = child[i].x;
-            stack[sp++] = child[i].y;
-            while (sp > 0)
-            {
-                const int c = stack[--sp];
-                if (c < 0 || flag[c])
-                {
-                    if (nc < 8)
-                        nd.child[nc] = c < 0 ? c : static_cast<int>(octidx[c]);
-                    else
-                        atomicOr(err, DEV_ERR_BOUNDS);
-                    ++nc;
-                }
-                else if (sp + 2 <= 8)
-                {
-                    stack[sp++] = child[c].x;
-                    stack[sp++] = child[c].y;
-                }
-                else
-                    atomicOr(err, DEV_ERR_BOUNDS);
-            }
-            nd.nchild = min(nc, 8);
+            const int2 ch = child[i];
+            collect_children<2>(ch.y, child, flag, octidx, out->child, nc, err);
+            collect_children<2>(ch.x, child, flag, octidx, out->child, nc, err);
+            nc = min(nc, 8);
         }
-        nodes[octidx[i]] = nd;
-        if (i == 0)
-            atomicAdd(&stats[2], static_cast<unsigned long long>(octidx[m - 1] + flag[m - 1]));
+        *reinterpret_cast<int4*>(&out->open_r2) = make_int4(__float_as_int(open_r2), nc, rg.x, rg.y);
     }
 
     // ------------------------------------------------------------------------------------
