@@ -686,7 +686,7 @@ def bench_reference(args):
         rate, cores, kind, sample = cpu_brute_force_rate(bodies, seconds=args.cpu_seconds / 2)
         info = (cores, kind, sample)
         if k >= args.warmup:
-            per_step.append(N / rate)     # seconds for one full body-step of all N bodies
+            per_step.append(float(N) * N / rate)    # seconds for one step: N^2 pairs at `rate` pairs/s
     total = sum(per_step)
     value = N * args.steps / total
     cores, kind, sample = info
