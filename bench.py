@@ -21,8 +21,10 @@ Printed JSON line (rank 0):
                   GPU FP64 form, itself checked against the CPU oracle on 512 targets).
   barnes_hut_16m  N = 16,777,216 exponential disk + Hernquist halo, eps = 0.005,
                   dt = 2.5e-4, FP32 tree forces + compensated integration, reference-
-                  convention theta 0.5 and 0.75: steps/s, interactions, tree cells, and the
-                  per-stage byte model against the measured HBM copy bandwidth.
+                  convention theta 0.5 and 0.75: steps/s, interactions, tree cells, the
+                  device time of the build and of the traversal (nbody_cuda_bh_stage_ms),
+                  the build's compulsory bytes against the measured HBM copy bandwidth,
+                  and the traversal's interactions (20 flop each) against the FFMA peak.
                   Its "transfer" object times the host transfer paths (staged, mapped,
                   direct) for all 16.8M Body records against the copy engine's pinned
                   bandwidth, and one frame of update + state().
@@ -403,6 +405,7 @@ def bench_bh16m(torch, stream, flush, native, scenes, args):
            "generate_s": gen_s, "theta_convention": "reference (accept when |com-x| > size*theta)"}
     with native.Context() as ctx:
         ctx.set_stream(stream.cuda_stream)
+        fp32_peak = max(ctx.calibrate_fp32())
         for theta in (0.5, 0.75):
             ctx.upload_bodies(b)
             p = native.params(mode=native.MODE_NLOGN, theta=theta, law=native.LAW_SOFTENED, eps2=0.005 ** 2,
@@ -412,23 +415,40 @@ def bench_bh16m(torch, stream, flush, native, scenes, args):
             torch.cuda.synchronize()
             steps = max(5, args.steps)
             ms = timed_steps(torch, stream, flush, lambda: ctx.update(p, 1), steps)
+            # the two stages of the accelerate, from the library's own stream events (one
+            # step at a time, after the timed region)
+            stage = []
+            for _ in range(3):
+                ctx.update(p, 1)
+                stage.append(ctx.bh_stage_ms())
+            build_ms = statistics.mean(s[0] for s in stage)
+            walk_ms = statistics.mean(s[1] for s in stage)
             ctx.accelerate(p)
             stats = ctx.bh_stats()
             ms_step = sum(ms) / steps
-            # compulsory bytes per step (byte model): bbox 16, Morton 16+8, sort 7 passes x 24,
-            # permute 32, build ~56 per internal node, COM ~48 per node, integrate 80 (+48 comp)
-            build_b = n * (16 + 24 + 7 * 24 + 32 + 56 + 48) + n * (80 + 48)
-            trav_b = 16 * stats["interactions"] + 64 * stats["visits"]
+            # compulsory HBM bytes per body of the build (byte model): bbox 16, Morton 16 + 8,
+            # sort 7 passes x 24, permute 32, tree ~56 per internal node, COM ~48 per node
+            build_bpb = 16 + 24 + 7 * 24 + 32 + 56 + 48
+            inter = stats["interactions"]
             res[f"theta_{theta}"] = {
                 "steps_per_s": 1e3 / ms_step, "ms_per_step": ms_step, "body_steps_per_s": n * 1e3 / ms_step,
-                "interactions": stats["interactions"], "interactions_per_body": stats["interactions"] / n,
+                "interactions": inter, "interactions_per_body": inter / n,
                 "warp_cell_visits": stats["visits"], "tree_cells": stats["cells"],
-                "roofline": {"bound": "hbm", "achieved": (build_b + trav_b) / (ms_step * 1e-3) / 1e9,
-                             "peak": hbm, "unit": "GB/s",
-                             "frac": (build_b + trav_b) / (ms_step * 1e-3) / 1e9 / hbm,
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs",
-                             "bytes_model": "build+integrate ~%d B/body, traversal 16 B/interaction + 64 B/cell "
-                                            "visit (mostly L2 hits)" % ((build_b) // n)},
+                "stage_ms": {"build": build_ms, "traversal": walk_ms,
+                             "integrate_and_rest": ms_step - build_ms - walk_ms,
+                             "source": "nbody_cuda_bh_stage_ms (CUDA events), mean of 3 steps"},
+                "roofline": {
+                    "build": {"bound": "hbm", "achieved": n * build_bpb / (build_ms * 1e-3) / 1e9, "peak": hbm,
+                              "unit": "GB/s", "frac": n * build_bpb / (build_ms * 1e-3) / 1e9 / hbm,
+                              "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                              "bytes_model": f"{build_bpb} B/body compulsory"},
+                    "traversal": {"bound": "issue (control flow of the walk; cells and bodies are L1/L2 hits)",
+                                  "achieved": FLOP_PER_PAIR * inter / (walk_ms * 1e-3) / 1e12, "peak": fp32_peak,
+                                  "unit": "TFLOP/s", "frac": FLOP_PER_PAIR * inter / (walk_ms * 1e-3) / 1e12 / fp32_peak,
+                                  "peak_source": "measured FFMA/FFMA2 chains (nbody_cuda_calibrate_fp32)",
+                                  "flop_model": f"{FLOP_PER_PAIR} flop per interaction, as the direct sum",
+                                  "interactions_per_s": inter / (walk_ms * 1e-3)},
+                },
             }
         p = native.params(mode=native.MODE_NLOGN, theta=0.5, law=native.LAW_SOFTENED, eps2=0.005 ** 2,
                           dt=2.5e-4, size=0.0, tree_box=1, precision=native.PREC_COMPENSATED)

@@ -289,6 +289,13 @@ int nbody_cuda_dev_accel_soa_noalloc(const void* pos_mass, const void* vel_radiu
  * cells built. Synchronous. */
 int nbody_cuda_bh_stats(nbody_cuda* ctx, uint64_t out[3]);
 
+/* Device time of the last Barnes-Hut accelerate's two stages, in milliseconds, from CUDA
+ * events on the context's stream: ms[0] = the tree build (root box, Morton codes, sort,
+ * cell sums, octree records), ms[1] = the traversal. NBODY_ERR_INVALID when no accelerate
+ * has been timed (none yet, or the last one was captured into a CUDA graph, where no
+ * events are recorded). Synchronous. No reference counterpart. */
+int nbody_cuda_bh_stage_ms(nbody_cuda* ctx, float ms[2]);
+
 /* Build the Barnes-Hut tree keys for the current bodies and copy back the Morton codes in
  * sorted order (codes, n entries), the sorted body order (order: the body index at each
  * sorted position; equal codes keep index order) and the root box (box: lower corner

@@ -11,7 +11,8 @@
 //      the reference's float centre comparisons choose (bounds.h:31-38), whose octant
 //      bit is set when the coordinate is below the centre: reference octant = digit ^ 7.
 //   3. radix_sort_pairs over (code, index): stable, so ties keep index order;
-//   4. gather_kernel: bodies into Morton order, plus FP64 prefix sums of m and m*(x - c);
+//   4. gather_kernel + cell_sum_kernel: bodies into Morton order, and exact fixed-point
+//      (int64) prefix sums of m and m*x, whose differences give each cell's mass and COM;
 //   5. karras_kernel: binary radix tree over the sorted codes (Karras 2012), duplicates
 //      separated by index; each internal node's common-prefix length fixes its octree
 //      level floor(prefix / 3) (capped at 21, the last Morton level);
@@ -46,8 +47,15 @@ namespace nbg
         constexpr int kMortonBits = 21;
         constexpr int kMaxLevel = 21;
         constexpr int kTravWarps = 8;
+        // warps per CTA of the walk with Q packed pairs per lane: its stack entries carry 2Q
+        // lane masks, and the stacks of one CTA stay within 48 KB of static shared memory
+        __host__ __device__ constexpr int pair_warps(const int q) { return q > 2 ? 4 : kTravWarps; }
         constexpr int kStack = 192;
         constexpr int kBboxBlocks = 1024;
+        constexpr int kBboxVals = 8;    // min x y z, max x y z, max |m|, max |x|
+        constexpr int kMomThreads = 1024;
+        constexpr int kMomItems = 4;
+        constexpr int kMomTile = kMomThreads * kMomItems;   // bodies per cell-sum tile
     }
 
     struct BhState
@@ -63,7 +71,7 @@ namespace nbg
         int* prefix = nullptr;          // common-prefix bits of each internal node
         uint32_t* octflag = nullptr;
         uint32_t* octidx = nullptr;
-        double4* psum = nullptr;        // N + 1 prefix sums
+        Int64x4* psum = nullptr;        // N + 1 fixed-point prefix sums of {m x, m y, m z, m}
         OctNode* nodes = nullptr;
         void* temp = nullptr;           // sort and scan temporaries
         size_t temp_bytes = 0;
@@ -73,6 +81,8 @@ namespace nbg
         const uint32_t* order = nullptr;       // sorted indices of the last build (keys/vals ping-pong)
         const uint64_t* codes = nullptr;
         bool built = false;                    // a tree for built_n bodies is on the device
+        cudaEvent_t ev[3] = { nullptr, nullptr, nullptr };  // build start, traversal start, end
+        bool timed = false;                    // ev[] bracket the last accelerate
         size_t built_n = 0;
         uint64_t build_id = 0;
     };
@@ -80,28 +90,33 @@ namespace nbg
     // ------------------------------------------------------------------------------------
     // 1. root box
     // ------------------------------------------------------------------------------------
-    __global__ void bbox_partial_kernel(const float4* __restrict__ src, const int stride, const int n,
-                                        double* __restrict__ part)
+    // Per block: the box's min and max per axis, and the largest finite |m| and |x| (over
+    // all axes), which fix the fixed-point scale of the cell sums. Min and max are exact,
+    // so the float fold equals a double one; the partials are widened at the end.
+    __global__ void __launch_bounds__(256) bbox_partial_kernel(const float4* __restrict__ src, const int stride,
+                                                               const int n, double* __restrict__ part)
     {
-        double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
+        float v[kBboxVals] = { INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.f, 0.f };
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         {
             const float4 p = src[static_cast<size_t>(i) * stride];
-            const double v[3] = { p.x, p.y, p.z };
+            const float m = stride == 3 ? src[static_cast<size_t>(i) * 3 + 1].w : p.w;
+            const float x[3] = { p.x, p.y, p.z };
 #pragma unroll
             for (int a = 0; a < 3; ++a)
             {
-                lo[a] = fmin(lo[a], v[a]);
-                hi[a] = fmax(hi[a], v[a]);
+                v[a] = fminf(v[a], x[a]);
+                v[3 + a] = fmaxf(v[3 + a], x[a]);
+                if (isfinite(x[a]))
+                    v[7] = fmaxf(v[7], fabsf(x[a]));
             }
+            if (isfinite(m))
+                v[6] = fmaxf(v[6], fabsf(m));
         }
-        __shared__ double red[6][256];
+        __shared__ float red[kBboxVals][256];
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
-        {
-            red[a][threadIdx.x] = lo[a];
-            red[3 + a][threadIdx.x] = hi[a];
-        }
+        for (int a = 0; a < kBboxVals; ++a)
+            red[a][threadIdx.x] = v[a];
         __syncthreads();
         for (int s = blockDim.x / 2; s > 0; s >>= 1)
         {
@@ -109,49 +124,64 @@ namespace nbg
             {
 #pragma unroll
                 for (int a = 0; a < 3; ++a)
-                {
-                    red[a][threadIdx.x] = fmin(red[a][threadIdx.x], red[a][threadIdx.x + s]);
-                    red[3 + a][threadIdx.x] = fmax(red[3 + a][threadIdx.x], red[3 + a][threadIdx.x + s]);
-                }
+                    red[a][threadIdx.x] = fminf(red[a][threadIdx.x], red[a][threadIdx.x + s]);
+#pragma unroll
+                for (int a = 3; a < kBboxVals; ++a)
+                    red[a][threadIdx.x] = fmaxf(red[a][threadIdx.x], red[a][threadIdx.x + s]);
             }
             __syncthreads();
         }
-        if (threadIdx.x < 6)
-            part[blockIdx.x * 6 + threadIdx.x] = red[threadIdx.x][0];
+        if (threadIdx.x < kBboxVals)
+            part[blockIdx.x * kBboxVals + threadIdx.x] = static_cast<double>(red[threadIdx.x][0]);
+    }
+
+    // The exponent e with 0 <= v < 2^e for a finite float v >= 0 (v = M 2^(E - 150) with
+    // M < 2^24, so v < 2^(E - 126); subnormals and zero lie below 2^-126).
+    __device__ __forceinline__ int bound_exp(const double v)
+    {
+        const uint32_t E = (__float_as_uint(static_cast<float>(v)) >> 23) & 0xffu;
+        return (E ? static_cast<int>(E) : 1) - 126;
     }
 
     __global__ void __launch_bounds__(256) box_final_kernel(const double* __restrict__ part, const int nparts,
-                                                            const int mode, const float size,
+                                                            const int n, const int mode, const float size,
                                                             BoxParams* __restrict__ box)
     {
         // one block folds the per-block partials (a strided pass, then a tree)
-        __shared__ double red[6][256];
-        double l[3] = { INFINITY, INFINITY, INFINITY }, h[3] = { -INFINITY, -INFINITY, -INFINITY };
+        __shared__ double red[kBboxVals][256];
+        double v[kBboxVals] = { INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.0, 0.0 };
         for (int k = threadIdx.x; k < nparts; k += blockDim.x)
-            for (int a = 0; a < 3; ++a)
-            {
-                l[a] = fmin(l[a], part[k * 6 + a]);
-                h[a] = fmax(h[a], part[k * 6 + 3 + a]);
-            }
-        for (int a = 0; a < 3; ++a)
         {
-            red[a][threadIdx.x] = l[a];
-            red[3 + a][threadIdx.x] = h[a];
+            for (int a = 0; a < 3; ++a)
+                v[a] = fmin(v[a], part[k * kBboxVals + a]);
+            for (int a = 3; a < kBboxVals; ++a)
+                v[a] = fmax(v[a], part[k * kBboxVals + a]);
         }
+        for (int a = 0; a < kBboxVals; ++a)
+            red[a][threadIdx.x] = v[a];
         __syncthreads();
         for (int s = blockDim.x / 2; s > 0; s >>= 1)
         {
             if (threadIdx.x < s)
+            {
                 for (int a = 0; a < 3; ++a)
-                {
                     red[a][threadIdx.x] = fmin(red[a][threadIdx.x], red[a][threadIdx.x + s]);
-                    red[3 + a][threadIdx.x] = fmax(red[3 + a][threadIdx.x], red[3 + a][threadIdx.x + s]);
-                }
+                for (int a = 3; a < kBboxVals; ++a)
+                    red[a][threadIdx.x] = fmax(red[a][threadIdx.x], red[a][threadIdx.x + s]);
+            }
             __syncthreads();
         }
         if (threadIdx.x != 0)
             return;
         BoxParams b;
+        // |m| < 2^em and |x| < 2^ex for every finite value, and n <= 2^cn, so
+        // n |m| 2^mass_shift and n |m x| 2^mom_shift stay below 2^61
+        const int cn = n > 1 ? 32 - __clz(n - 1) : 0;
+        const int m_exp = bound_exp(red[6][0]), x_exp = bound_exp(red[7][0]);
+        b.mass_shift = 61 - cn - m_exp;
+        b.mom_shift = 61 - cn - m_exp - x_exp;
+        b.mass_unit = ldexp(1.0, -b.mass_shift);
+        b.com_unit = ldexp(1.0, x_exp);
         if (mode == 0)
         {
             // tree.h:20 / bhtree.h:29: centred at the origin, edge State::size
@@ -299,40 +329,193 @@ namespace nbg
     }
 
     // ------------------------------------------------------------------------------------
-    // 4. Morton-ordered copies and FP64 prefix-sum inputs
+    // 4. Morton-ordered copies and the fixed-point cell sums
     // ------------------------------------------------------------------------------------
-    __global__ void gather_kernel(const float4* __restrict__ src, const int stride,
-                                  const float4* __restrict__ vel_radius, const uint32_t* __restrict__ order,
-                                  const int n, const BoxParams* __restrict__ box, float4* __restrict__ spm,
-                                  float* __restrict__ srad, double4* __restrict__ psum)
+    // A cell's mass and centre of mass come from differences of prefix sums over the sorted
+    // bodies. The sums are integers -- each body's m 2^mass_shift and m x 2^mom_shift,
+    // rounded once -- so a difference is the exact sum of the cell's rounded terms: no
+    // cancellation against the large prefixes before it, and the same bits whatever order
+    // the additions run in. A body's term is formed from the float significands with
+    // integer multiplies (m x is an exact 48-bit product), without FP64 arithmetic.
+
+    // v = M 2^e with M < 2^24 (the significand, implicit bit included); false for inf/NaN
+    __device__ __forceinline__ bool split_float(const float v, uint32_t& M, int& e, bool& neg)
     {
-        const int k = blockIdx.x * blockDim.x + threadIdx.x;
-        if (k > n)
-            return;
-        if (k == n)
-        {
-            psum[n] = make_double4(0, 0, 0, 0);
-            return;
-        }
-        const uint32_t i = order[k];
-        const float4 p = src[static_cast<size_t>(i) * stride];
-        float m, r;
-        if (stride == 3)
-        {
-            m = src[static_cast<size_t>(i) * 3 + 1].w;    // Body: {pos, radius}, {vel, mass}
-            r = p.w;
-        }
+        const uint32_t bits = __float_as_uint(v);
+        const uint32_t E = (bits >> 23) & 0xffu;
+        neg = (bits >> 31) != 0;
+        M = E ? ((bits & 0x7fffffu) | 0x800000u) : (bits & 0x7fffffu);
+        e = (E ? static_cast<int>(E) : 1) - 150;
+        return E != 0xffu;
+    }
+
+    // round(P 2^s), halves away from zero, with the sign applied. P < 2^48; the box's shifts
+    // keep P 2^s below 2^61, so a left shift never overflows (and s >= 64 only when P = 0).
+    __device__ __forceinline__ long long fixed_round(const uint64_t P, const int s, const bool neg)
+    {
+        uint64_t q;
+        if (s >= 0)
+            q = s < 64 ? P << s : 0;
+        else if (s > -50)
+            q = (P + (1ull << (-s - 1))) >> -s;
         else
+            q = 0;      // P 2^s < 2^-2
+        return neg ? -static_cast<long long>(q) : static_cast<long long>(q);
+    }
+
+    // {m x, m y, m z, m} of one body in the box's fixed-point units. A non-finite mass
+    // contributes nothing; a non-finite coordinate contributes no moment on its axis.
+    __device__ __forceinline__ Int64x4 body_terms(const float4 pm, const int mass_shift, const int mom_shift)
+    {
+        uint32_t Mm;
+        int em;
+        bool nm;
+        if (!split_float(pm.w, Mm, em, nm))
+            return Int64x4{ 0, 0, 0, 0 };
+        const float x[3] = { pm.x, pm.y, pm.z };
+        long long q[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
         {
-            m = p.w;
-            r = vel_radius ? vel_radius[i].w : 0.f;
+            uint32_t Mx;
+            int ex;
+            bool nx;
+            q[a] = split_float(x[a], Mx, ex, nx)
+                       ? fixed_round(static_cast<uint64_t>(Mm) * Mx, em + ex + mom_shift, nm != nx) : 0;
         }
-        spm[k] = make_float4(p.x, p.y, p.z, m);
-        srad[k] = r;
-        const double dm = m;
-        psum[k] = make_double4(dm * (static_cast<double>(p.x) - box->center[0]),
-                               dm * (static_cast<double>(p.y) - box->center[1]),
-                               dm * (static_cast<double>(p.z) - box->center[2]), dm);
+        return Int64x4{ q[0], q[1], q[2], fixed_round(Mm, em + mass_shift, nm) };
+    }
+
+    __device__ __forceinline__ Int64x4 add4(const Int64x4 a, const Int64x4 b)
+    {
+        return Int64x4{ a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w };
+    }
+
+    // Bodies into Morton order (pos_mass, and the radius when srad is given: only the cutoff
+    // law reads it), and the total of each tile's terms.
+    __global__ void __launch_bounds__(kMomThreads) gather_kernel(
+        const float4* __restrict__ src, const int stride, const float4* __restrict__ vel_radius,
+        const uint32_t* __restrict__ order, const int n, const BoxParams* __restrict__ box,
+        float4* __restrict__ spm, float* __restrict__ srad, Int64x4* __restrict__ tile_sum)
+    {
+        Int64x4 t{ 0, 0, 0, 0 };
+        if (n > 0)
+        {
+            const int mass_shift = box->mass_shift, mom_shift = box->mom_shift;
+            // all of a thread's random reads are issued before any is used (indices past
+            // the end read the last body and are not stored)
+            float4 p[kMomItems];
+            float m[kMomItems], r[kMomItems];
+#pragma unroll
+            for (int j = 0; j < kMomItems; ++j)
+            {
+                const int k = min(blockIdx.x * kMomTile + j * kMomThreads + static_cast<int>(threadIdx.x), n - 1);
+                const uint32_t i = order[k];
+                p[j] = src[static_cast<size_t>(i) * stride];
+                if (stride == 3)
+                {
+                    m[j] = src[static_cast<size_t>(i) * 3 + 1].w;     // Body: {pos, radius}, {vel, mass}
+                    r[j] = p[j].w;
+                }
+                else
+                {
+                    m[j] = p[j].w;
+                    r[j] = vel_radius ? vel_radius[i].w : 0.f;
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < kMomItems; ++j)
+            {
+                const int k = blockIdx.x * kMomTile + j * kMomThreads + threadIdx.x;
+                if (k < n)
+                {
+                    const float4 pm = make_float4(p[j].x, p[j].y, p[j].z, m[j]);
+                    spm[k] = pm;
+                    if (srad)
+                        srad[k] = r[j];
+                    t = add4(t, body_terms(pm, mass_shift, mom_shift));
+                }
+            }
+        }
+        using Op = ScanOps<Int64x4>;
+        for (int d = 16; d > 0; d >>= 1)
+            t = add4(t, Op::shfl_down(t, d));
+        __shared__ Int64x4 warp_sum[kMomThreads / 32];
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (lane == 0)
+            warp_sum[warp] = t;
+        __syncthreads();
+        if (warp == 0)
+        {
+            t = warp_sum[lane];
+            for (int d = 16; d > 0; d >>= 1)
+                t = add4(t, Op::shfl_down(t, d));
+            if (lane == 0)
+                tile_sum[blockIdx.x] = t;
+        }
+    }
+
+    // psum[k] = the sum of the terms of sorted bodies 0 .. k-1, for k = 0 .. n: each tile
+    // scans its own terms (recomputed from the sorted copy) from its offset, the exclusive
+    // scan of the tile totals.
+    __global__ void __launch_bounds__(kMomThreads) cell_sum_kernel(
+        const float4* __restrict__ spm, const int n, const BoxParams* __restrict__ box,
+        const Int64x4* __restrict__ tile_off, Int64x4* __restrict__ psum)
+    {
+        using Op = ScanOps<Int64x4>;
+        const int mass_shift = box->mass_shift, mom_shift = box->mom_shift;
+        const int base = blockIdx.x * kMomTile + threadIdx.x * kMomItems;
+        Int64x4 v[kMomItems];
+        Int64x4 run{ 0, 0, 0, 0 };
+#pragma unroll
+        for (int k = 0; k < kMomItems; ++k)
+        {
+            const int i = base + k;
+            const Int64x4 q = i < n ? body_terms(spm[i], mass_shift, mom_shift) : Int64x4{ 0, 0, 0, 0 };
+            v[k] = run;
+            run = add4(run, q);
+        }
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        Int64x4 incl = run;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1)
+        {
+            const Int64x4 o = Op::shfl_up(incl, d);
+            if (lane >= d)
+                incl = add4(incl, o);
+        }
+        __shared__ Int64x4 warp_tot[kMomThreads / 32];
+        if (lane == 31)
+            warp_tot[warp] = incl;
+        __syncthreads();
+        if (warp == 0)
+        {
+            Int64x4 wi = warp_tot[lane];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1)
+            {
+                const Int64x4 o = Op::shfl_up(wi, d);
+                if (lane >= d)
+                    wi = add4(wi, o);
+            }
+            warp_tot[lane] = wi;    // inclusive over warps
+        }
+        __syncthreads();
+        Int64x4 excl = Op::shfl_up(incl, 1);
+        if (lane == 0)
+            excl = Int64x4{ 0, 0, 0, 0 };
+        Int64x4 off = add4(tile_off[blockIdx.x], excl);
+        if (warp > 0)
+            off = add4(off, warp_tot[warp - 1]);
+#pragma unroll
+        for (int k = 0; k < kMomItems; ++k)
+        {
+            const int i = base + k;
+            if (i < n)
+                psum[i] = add4(off, v[k]);
+        }
+        if (base <= n - 1 && n - 1 < base + kMomItems)
+            psum[n] = add4(off, run);
     }
 
     // ------------------------------------------------------------------------------------
@@ -431,9 +614,10 @@ namespace nbg
         collect_children<DEPTH ? DEPTH - 1 : 0>(ch.x, child, flag, octidx, out, nc, err);
     }
 
-    __global__ void octnode_kernel(const int2* __restrict__ child, const int2* __restrict__ range,
+    // latency bound (chains of dependent loads): full occupancy, 32 registers
+    __global__ void __launch_bounds__(256, 7) octnode_kernel(const int2* __restrict__ child, const int2* __restrict__ range,
                                    const int* __restrict__ prefix, const uint32_t* __restrict__ flag,
-                                   const uint32_t* __restrict__ octidx, const double4* __restrict__ psum,
+                                   const uint32_t* __restrict__ octidx, const Int64x4* __restrict__ psum,
                                    const int m, const BoxParams* __restrict__ box, const float theta,
                                    OctNode* __restrict__ nodes, unsigned* __restrict__ err,
                                    unsigned long long* __restrict__ stats)
@@ -446,16 +630,17 @@ namespace nbg
         const int2 rg = range[i];
         const int pre = prefix[i];
         const int lvl = level_of(pre);
-        const double4 hi = psum[rg.y + 1], lo = psum[rg.x];
-        const double ms = hi.w - lo.w;
+        const Int64x4 hi = psum[rg.y + 1], lo = psum[rg.x];
+        const long long ms = hi.w - lo.w;   // exact: the cell's own terms
         OctNode* out = nodes + octidx[i];
-        if (ms > 0.0)
+        if (ms > 0)
         {
-            const double inv = 1.0 / ms;
-            out->com_mass = make_float4(static_cast<float>(box->center[0] + (hi.x - lo.x) * inv),
-                                        static_cast<float>(box->center[1] + (hi.y - lo.y) * inv),
-                                        static_cast<float>(box->center[2] + (hi.z - lo.z) * inv),
-                                        static_cast<float>(ms));
+            // com = (sum of m x 2^mom_shift) / (sum of m 2^mass_shift) * 2^(mass_shift - mom_shift)
+            const double inv = box->com_unit / static_cast<double>(ms);
+            out->com_mass = make_float4(static_cast<float>(static_cast<double>(hi.x - lo.x) * inv),
+                                        static_cast<float>(static_cast<double>(hi.y - lo.y) * inv),
+                                        static_cast<float>(static_cast<double>(hi.z - lo.z) * inv),
+                                        static_cast<float>(static_cast<double>(ms) * box->mass_unit));
         }
         else
             out->com_mass = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -672,7 +857,7 @@ namespace nbg
     // depth-first order, so its sum is the one traverse_kernel forms; one walk now serves
     // 2Q times the targets and every interaction is a packed pair.
     template <int LAW, int Q>
-    __global__ void __launch_bounds__(kTravWarps * 32, 2) traverse_pairs_kernel(
+    __global__ void __launch_bounds__(pair_warps(Q) * 32, 2 * kTravWarps / pair_warps(Q)) traverse_pairs_kernel(
         const OctNode* __restrict__ nodes, const float4* __restrict__ spm, const float* __restrict__ srad,
         const uint32_t* __restrict__ order, const int n, const float G, const float eps2,
         float4* __restrict__ acc, float* __restrict__ body_out, unsigned* __restrict__ err,
@@ -680,13 +865,14 @@ namespace nbg
     {
         constexpr int H = 2 * Q;                    // target slots per lane
         constexpr int TW = 32 * H;                  // targets per warp walk
-        __shared__ int stk_cell[kTravWarps][kStack];
-        __shared__ unsigned stk_mask[kTravWarps][kStack][H];    // lanes of each slot that opened it
+        constexpr int W = pair_warps(Q);
+        __shared__ int stk_cell[W][kStack];
+        __shared__ unsigned stk_mask[W][kStack][H];     // lanes of each slot that opened it
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         const unsigned lt = (1u << lane) - 1u;
         unsigned inter = 0, visits = 0;
 
-        for (int tile = blockIdx.x * kTravWarps + warp; tile * TW < n; tile += gridDim.x * kTravWarps)
+        for (int tile = blockIdx.x * W + warp; tile * TW < n; tile += gridDim.x * W)
         {
             float2 npx[Q], npy[Q], npz[Q], lim[Q], ax[Q], ay[Q], az[Q];
             unsigned m0[H];
@@ -756,7 +942,6 @@ namespace nbg
                     continue;       // bhtree.cpp:109-113: empty nodes are skipped
                 const float open_r2 = __int_as_float(meta.x);
                 bool take[H];
-                bool any_take = false;
                 unsigned open_any = 0;
                 unsigned open[H];
 #pragma unroll
@@ -783,9 +968,7 @@ namespace nbg
                 {
                     open[h] = mask[h] & ~__ballot_sync(0xffffffffu, take[h]);
                     open_any |= open[h];
-                    any_take |= take[h];
                 }
-                (void)any_take;
                 if (!open_any)
                     continue;
                 bool mine[H], mine_any = false;
@@ -915,7 +1098,8 @@ namespace nbg
             {
                 cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&b.box), sizeof(BoxParams), ctx->stream);
                 if (e == cudaSuccess)
-                    e = cudaMallocAsync(reinterpret_cast<void**>(&b.bbox_part), kBboxBlocks * 6 * sizeof(double), ctx->stream);
+                    e = cudaMallocAsync(reinterpret_cast<void**>(&b.bbox_part), kBboxBlocks * kBboxVals * sizeof(double),
+                                        ctx->stream);
                 if (e == cudaSuccess)
                     e = cudaMallocAsync(reinterpret_cast<void**>(&b.stats), 4 * sizeof(unsigned long long), ctx->stream);
                 if (e != cudaSuccess)
@@ -926,7 +1110,8 @@ namespace nbg
             if (const int st = before_allocation(ctx))
                 return st;
             const size_t cap = std::max(n, b.cap + b.cap / 2);
-            const size_t tb = std::max(sort_temp_bytes(cap), scan_temp_elems(cap + 1) * sizeof(double4));
+            const size_t tiles = (cap + kMomTile - 1) / kMomTile;
+            const size_t tb = std::max(sort_temp_bytes(cap), (tiles + scan_temp_elems(tiles)) * sizeof(Int64x4));
             cudaError_t e = cudaSuccess;
             cudaStream_t s = ctx->stream;
             for (int k = 0; k < 2 && e == cudaSuccess; ++k)
@@ -990,29 +1175,34 @@ namespace nbg
         cudaMemsetAsync(b.stats, 0, 4 * sizeof(unsigned long long), s);
         // tree_box = 0 is the reference's fixed root box; it needs a positive size
         const bool auto_box = p->tree_box != 0 || !(p->size > 0.f);
-        if (auto_box)
-        {
-            bbox_partial_kernel<<<kBboxBlocks, 256, 0, s>>>(src, stride, ni, b.bbox_part);
-            ++L;
-        }
-        box_final_kernel<<<1, 256, 0, s>>>(b.bbox_part, auto_box ? kBboxBlocks : 0, auto_box ? 1 : 0, p->size, b.box);
+        // the bounds pass runs for the fixed box too: the cell sums' scale comes from it
+        bbox_partial_kernel<<<kBboxBlocks, 256, 0, s>>>(src, stride, ni, b.bbox_part);
+        ++L;
+        box_final_kernel<<<1, 256, 0, s>>>(b.bbox_part, kBboxBlocks, ni, auto_box ? 1 : 0, p->size, b.box);
         ++L;
         morton_kernel<<<blocks, 256, 0, s>>>(src, stride, ni, b.box, b.keys[0], b.vals[0]);
         ++L;
         bool in_alt = false;
-        cudaError_t e = radix_sort_pairs(b.keys[0], b.vals[0], b.keys[1], b.vals[1], n, 0, 63, b.temp, s, &L, &in_alt);
+        cudaError_t e = radix_sort_pairs(b.keys[0], b.vals[0], b.keys[1], b.vals[1], n, 0, 63, b.temp, s, &L, &in_alt,
+                                         ctx->dev_error);
         if (e != cudaSuccess)
             return ctx_cuda_fail(ctx, e, "radix sort");
         const uint64_t* keys = b.keys[in_alt ? 1 : 0];
         const uint32_t* order = b.vals[in_alt ? 1 : 0];
         b.order = order;
         b.codes = keys;
-        gather_kernel<<<ceil_div(n + 1, 256), 256, 0, s>>>(src, stride, ctx->layout == NBODY_LAYOUT_AOS ? nullptr : ctx->vr,
-                                                            order, ni, b.box, b.spm, b.srad, b.psum);
+        const unsigned tiles = std::max(1u, ceil_div(n, kMomTile));
+        Int64x4* tile_sum = static_cast<Int64x4*>(b.temp);
+        const bool radius = p->law == NBODY_LAW_CUTOFF;
+        gather_kernel<<<tiles, kMomThreads, 0, s>>>(src, stride,
+                                                    radius && ctx->layout != NBODY_LAYOUT_AOS ? ctx->vr : nullptr,
+                                                    order, ni, b.box, b.spm, radius ? b.srad : nullptr, tile_sum);
         ++L;
-        e = exclusive_scan<double4>(b.psum, b.psum, n + 1, static_cast<double4*>(b.temp), s, &L);
+        e = exclusive_scan<Int64x4>(tile_sum, tile_sum, tiles, tile_sum + tiles, s, &L);
         if (e != cudaSuccess)
-            return ctx_cuda_fail(ctx, e, "prefix sums");
+            return ctx_cuda_fail(ctx, e, "cell sums");
+        cell_sum_kernel<<<tiles, kMomThreads, 0, s>>>(b.spm, ni, b.box, tile_sum, b.psum);
+        ++L;
         if (n < 2)
         {
             b.built = true;
@@ -1043,10 +1233,22 @@ namespace nbg
     int bh_accelerate(nbody_cuda* ctx, const nbody_step_params* p)
     {
         const size_t n = ctx->count;
+        if (!ctx->bh)
+            ctx->bh = new BhState();
+        // stage timing: three events on the stream, except while it is captured into a graph
+        cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+        bool timed = cudaStreamIsCapturing(ctx->stream, &capture) == cudaSuccess && capture == cudaStreamCaptureStatusNone;
+        for (int k = 0; k < 3 && timed; ++k)
+            timed = ctx->bh->ev[k] || cudaEventCreate(&ctx->bh->ev[k]) == cudaSuccess;
+        ctx->bh->timed = false;
+        if (timed)
+            cudaEventRecord(ctx->bh->ev[0], ctx->stream);
         if (const int st = bh_build(ctx, p))
             return st;
         BhState& b = *ctx->bh;
         cudaStream_t s = ctx->stream;
+        if (timed)
+            cudaEventRecord(b.ev[1], s);
         const int ni = static_cast<int>(n);
         float4* acc = ctx->layout == NBODY_LAYOUT_AOS ? nullptr : ctx->acc;
         float* body_out = ctx->layout == NBODY_LAYOUT_AOS ? ctx->bodies : nullptr;
@@ -1066,21 +1268,34 @@ namespace nbg
         // NBODY_CUDA_BH_TARGETS=32 asks for the one-target-per-lane walk; all give the same sums
         const char* tsel = std::getenv("NBODY_CUDA_BH_TARGETS");
         const int per_warp = tsel ? std::atoi(tsel) : 128;
-        if (per_warp == 64 || per_warp == 128)
+        if (per_warp == 64 || per_warp == 128 || per_warp == 256)
         {
             const bool soft = p->law == NBODY_LAW_SOFTENED;
-            auto fn = per_warp == 128 ? (soft ? traverse_pairs_kernel<NBODY_LAW_SOFTENED, 2> : traverse_pairs_kernel<NBODY_LAW_CUTOFF, 2>)
-                                      : (soft ? traverse_pairs_kernel<NBODY_LAW_SOFTENED, 1> : traverse_pairs_kernel<NBODY_LAW_CUTOFF, 1>);
+            using Walk = void (*)(const OctNode*, const float4*, const float*, const uint32_t*, int, float, float,
+                                  float4*, float*, unsigned*, unsigned long long*);
+            Walk fn;
+            int warps = kTravWarps;
+            if (per_warp == 256)
+            {
+                fn = soft ? traverse_pairs_kernel<NBODY_LAW_SOFTENED, 4> : traverse_pairs_kernel<NBODY_LAW_CUTOFF, 4>;
+                warps = pair_warps(4);
+            }
+            else if (per_warp == 128)
+                fn = soft ? traverse_pairs_kernel<NBODY_LAW_SOFTENED, 2> : traverse_pairs_kernel<NBODY_LAW_CUTOFF, 2>;
+            else
+                fn = soft ? traverse_pairs_kernel<NBODY_LAW_SOFTENED, 1> : traverse_pairs_kernel<NBODY_LAW_CUTOFF, 1>;
             // one resident wave of CTAs: the grid-stride loop gives every CTA the same number
             // of tiles, so a second, partial wave would leave most SMs idle
             int per = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kTravWarps * 32, 0) != cudaSuccess || per < 1)
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, warps * 32, 0) != cudaSuccess || per < 1)
                 per = 1;
             const int tiles2 = (ni + per_warp - 1) / per_warp;
-            const int grid2 = std::min((tiles2 + kTravWarps - 1) / kTravWarps, sms * per);
-            fn<<<grid2, kTravWarps * 32, 0, s>>>(b.nodes, b.spm, b.srad, b.order, ni, p->G, p->eps2, acc, body_out,
-                                                  ctx->dev_error, b.stats);
+            const int grid2 = std::min((tiles2 + warps - 1) / warps, sms * per);
+            fn<<<grid2, warps * 32, 0, s>>>(b.nodes, b.spm, b.srad, b.order, ni, p->G, p->eps2, acc, body_out,
+                                             ctx->dev_error, b.stats);
             ++ctx->launches;
+            if (timed)
+                b.timed = cudaEventRecord(b.ev[2], s) == cudaSuccess;
             const cudaError_t e2 = cudaGetLastError();
             return e2 == cudaSuccess ? NBODY_OK : ctx_cuda_fail(ctx, e2, "tree traversal");
         }
@@ -1093,10 +1308,27 @@ namespace nbg
             traverse_kernel<NBODY_LAW_CUTOFF><<<grid, kTravWarps * 32, 0, s>>>(
                 b.nodes, b.spm, b.srad, b.order, ni, p->G, p->eps2, acc, body_out, ctx->dev_error, b.stats);
         ++ctx->launches;
+        if (timed)
+            b.timed = cudaEventRecord(b.ev[2], s) == cudaSuccess;
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess)
             return ctx_cuda_fail(ctx, e, "tree traversal");
         return NBODY_OK;
+    }
+
+    int bh_stage_ms(nbody_cuda* ctx, float ms[2])
+    {
+        if (!ctx->bh || !ctx->bh->timed)
+            return ctx_fail(ctx, NBODY_ERR_INVALID, "no timed Barnes-Hut accelerate");
+        BhState& b = *ctx->bh;
+        cudaError_t e = cudaEventSynchronize(b.ev[2]);
+        if (e == cudaSuccess)
+            e = cudaEventElapsedTime(&ms[0], b.ev[0], b.ev[1]);
+        if (e == cudaSuccess)
+            e = cudaEventElapsedTime(&ms[1], b.ev[1], b.ev[2]);
+        if (e != cudaSuccess)
+            return ctx_cuda_fail(ctx, e, "stage timing");
+        return check_device_error(ctx);
     }
 
     void release_bh(nbody_cuda* ctx)
@@ -1113,6 +1345,9 @@ namespace nbg
                          b.nodes, b.temp, b.box, b.bbox_part, b.stats };
         for (void* q : ptrs)
             cudaFree(q);
+        for (cudaEvent_t ev : b.ev)
+            if (ev)
+                cudaEventDestroy(ev);
         delete ctx->bh;
         ctx->bh = nullptr;
     }

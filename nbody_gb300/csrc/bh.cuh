@@ -15,7 +15,7 @@ namespace nbg
     struct BoxParams
     {
         double lo[3];       // lower corner
-        double center[3];   // centre (prefix sums are taken relative to it)
+        double center[3];   // centre
         double edge;        // cube edge
         double inv_cell;    // 2^21 / edge
         // When the edge is a power of two and the corner lies on the cell grid, the cell
@@ -23,6 +23,13 @@ namespace nbg
         int exact;
         int cell_exp;               // log2(edge / 2^21)
         long long lo_cells[3];      // lo / cell
+        // Fixed-point cell sums: a body's mass is summed as the integer m 2^mass_shift and
+        // its moment as m x 2^mom_shift, both rounded; the shifts keep every sum of all n
+        // bodies below 2^61 (from the largest finite |m| and |x|, see box_final_kernel).
+        int mass_shift;
+        int mom_shift;
+        double mass_unit;   // 2^-mass_shift: the mass of one fixed-point unit
+        double com_unit;    // 2^(mass_shift - mom_shift): moment units per mass unit
     };
 
     // One octree cell: 64 bytes, read whole by a warp (a broadcast load per field).
@@ -51,5 +58,6 @@ namespace nbg
     int bh_download(nbody_cuda* ctx, TreeSnapshot* out);
     uint64_t bh_build_id(const nbody_cuda* ctx);    // 0 before the first build
     int bh_stats(nbody_cuda* ctx, unsigned long long out[3]);
+    int bh_stage_ms(nbody_cuda* ctx, float ms[2]);
     int bh_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* codes, uint32_t* order, double box[4]);
 }

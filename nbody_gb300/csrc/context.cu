@@ -648,6 +648,13 @@ int nbody_cuda_bh_stats(nbody_cuda* ctx, uint64_t out[3])
     return st;
 }
 
+int nbody_cuda_bh_stage_ms(nbody_cuda* ctx, float ms[2])
+{
+    if (!ctx || !ms)
+        return NBODY_ERR_INVALID;
+    return bh_stage_ms(ctx, ms);
+}
+
 int nbody_cuda_morton(nbody_cuda* ctx, const nbody_step_params* p, uint64_t* codes, uint32_t* order, double box[4])
 {
     if (!ctx)

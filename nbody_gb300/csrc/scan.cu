@@ -111,5 +111,5 @@ namespace nbg
     }
 
     template cudaError_t exclusive_scan<uint32_t>(const uint32_t*, uint32_t*, size_t, uint32_t*, cudaStream_t, uint64_t*);
-    template cudaError_t exclusive_scan<double4>(const double4*, double4*, size_t, double4*, cudaStream_t, uint64_t*);
+    template cudaError_t exclusive_scan<Int64x4>(const Int64x4*, Int64x4*, size_t, Int64x4*, cudaStream_t, uint64_t*);
 }

@@ -1,20 +1,28 @@
-// LSD radix sort of (uint64 key, uint32 value) pairs, 9-bit digits, stable.
+// LSD radix sort of (uint64 key, uint32 value) pairs, 9-bit digits, stable, one kernel per
+// digit pass (a onesweep-style sort: Adinets & Merrill 2022).
 //
-// Seven passes cover a 63-bit Morton code exactly. One pass, three steps:
-//   1. digit_count: each CTA histograms the digits of its 4096-key tile into
-//      counts[digit * tiles + tile] (digit-major, so one exclusive scan of the whole
-//      array gives every (digit, tile) its global output offset);
-//   2. exclusive scan of counts (scan.cu);
-//   3. digit_scatter: each CTA re-reads its tile, ranks every key stably among the tile's
-//      equal digits, stages the tile in shared memory in digit order, and writes it out
-//      so that each digit's run of keys lands contiguously (coalesced stores).
+// Seven passes cover a 63-bit Morton code exactly.
+//   0. digit_hist: one read of the keys histograms the digits of every pass at once (a
+//      key's digits do not depend on the order of the keys), into ghist[pass][digit].
+//   1. digit_pass (once per pass): a CTA takes the next 4096-key tile in launch order (an
+//      atomic ticket), ranks its keys stably, publishes its per-digit counts, and finds
+//      how many keys of each digit the earlier tiles hold by decoupled look-back over
+//      their published counts. The tile is staged in shared memory in digit order and
+//      written out so that each digit's run lands contiguously (coalesced stores).
+// The look-back only waits on tiles whose tickets were taken earlier, by CTAs that are
+// already running and that publish their counts before they wait themselves, so the wait
+// always ends; it is still bounded in time, and a wait that gives up records
+// DEV_ERR_TIMEOUT. Counts are exact integers, so the result does not depend on timing.
 // Stability: warp w of a CTA owns the contiguous slice [w*512, (w+1)*512) of the tile and
 // walks it in 16 rounds of 32 consecutive keys; a key's rank is (equal digits in earlier
 // warps) + (equal digits in earlier rounds of its warp) + (equal digits on lower lanes of
-// its round, from __match_any_sync). Equal keys therefore keep their input order, and a
+// its round, from __match_any_sync). A round's per-warp count is taken and advanced by one
+// shared-memory atomic of the round's leader lane; a warp's atomics complete in program
+// order, so rounds count in order. Equal keys therefore keep their input order, and a
 // sort of (code, index) pairs starting from index order yields the order by (code, index).
+#include <algorithm>
+
 #include "common.cuh"
-#include "scan.cuh"
 #include "sort.cuh"
 
 namespace nbg
@@ -28,90 +36,178 @@ namespace nbg
         constexpr int kBits = 9;
         constexpr int kDigits = 1 << kBits;
         constexpr unsigned kMask = kDigits - 1;
+        constexpr int kPer = kDigits / kThreads;      // digits per thread in the per-digit steps
+        constexpr int kMaxPasses = 8;
+        constexpr int kHistThreads = 1024;
 
-        // dynamic shared memory of the scatter: per-warp counters, digit starts within the
-        // tile, global offsets, and the staged keys and values
-        constexpr size_t kScatterSmem = sizeof(uint32_t) * (kWarps * kDigits + 2 * kDigits)
-                                        + sizeof(uint64_t) * kTile + sizeof(uint32_t) * kTile;
+        // A tile's published count for one digit: flag in bits 62-63, the pass's epoch
+        // (pass + 1) in bits 32-61, the count in bits 0-31. A word from an earlier pass (or
+        // the zeroed array) has another epoch and reads as not yet published.
+        constexpr uint64_t kFlagAggregate = 1ull << 62;    // this tile's own count
+        constexpr uint64_t kFlagInclusive = 2ull << 62;    // count of this and all earlier tiles
+
+        // dynamic shared memory of a pass: staged keys and values, per-warp counters, digit
+        // starts within the tile and global digit bases
+        constexpr size_t kPassSmem = sizeof(uint64_t) * kTile + sizeof(uint32_t) * kTile
+                                     + sizeof(uint32_t) * (kWarps * kDigits + 2 * kDigits);
+
+        struct TempLayout
+        {
+            uint32_t* tickets;      // kMaxPasses tile tickets
+            uint32_t* ghist;        // kMaxPasses x kDigits global digit counts
+            uint64_t* status;       // tiles x kDigits published counts
+            size_t zero_bytes;      // everything above is zeroed before a sort
+        };
+
+        constexpr size_t kGhistOffset = 256;
+        constexpr size_t kStatusOffset = kGhistOffset + sizeof(uint32_t) * kMaxPasses * kDigits;
+
+        size_t zero_bytes(const size_t tiles) { return kStatusOffset + sizeof(uint64_t) * tiles * kDigits; }
+
+        TempLayout layout(void* temp, const size_t tiles)
+        {
+            TempLayout t;
+            unsigned char* p = static_cast<unsigned char*>(temp);
+            t.tickets = reinterpret_cast<uint32_t*>(p);
+            t.ghist = reinterpret_cast<uint32_t*>(p + kGhistOffset);
+            t.status = reinterpret_cast<uint64_t*>(p + kStatusOffset);
+            t.zero_bytes = zero_bytes(tiles);
+            return t;
+        }
     }
 
-    __global__ void __launch_bounds__(kThreads) digit_count_kernel(const uint64_t* __restrict__ keys, const int n,
-                                                                   const int shift, const int tiles,
-                                                                   uint32_t* __restrict__ counts)
+    // Histograms of the digits of all passes, in one read of the keys.
+    __global__ void __launch_bounds__(kHistThreads) digit_hist_kernel(const uint64_t* __restrict__ keys, const int n,
+                                                                      const int shift0, const int passes,
+                                                                      uint32_t* __restrict__ ghist)
     {
-        __shared__ uint32_t hist[kDigits];
-        for (int d = threadIdx.x; d < kDigits; d += kThreads)
+        __shared__ uint32_t hist[kMaxPasses * kDigits];
+        for (int d = threadIdx.x; d < passes * kDigits; d += kHistThreads)
             hist[d] = 0;
         __syncthreads();
-        // Warp-aggregated: one shared atomic per distinct digit per 32 keys (the top digits
-        // of Morton codes are often all equal, which would serialise per-key atomics).
-        const int base = blockIdx.x * kTile;
-        const int lane = threadIdx.x & 31;
-        for (int k = threadIdx.x; k < kTile; k += kThreads)
+        const int stride = gridDim.x * kHistThreads;
+        int i = blockIdx.x * kHistThreads + threadIdx.x;
+        // four keys in flight per thread
+        for (; static_cast<long long>(i) + 3 * stride < n; i += 4 * stride)
         {
-            const int i = base + k;
-            const bool ok = i < n;
-            const unsigned d = ok ? static_cast<unsigned>((keys[i] >> shift) & kMask) : static_cast<unsigned>(kDigits);
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
-            if (ok && lane == __ffs(peers) - 1)
-                atomicAdd(&hist[d], static_cast<uint32_t>(__popc(peers)));
+            uint64_t k[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                k[u] = keys[i + u * stride];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                for (int p = 0; p < passes; ++p)
+                    atomicAdd(&hist[p * kDigits + static_cast<int>((k[u] >> (shift0 + p * kBits)) & kMask)], 1u);
+        }
+        for (; i < n; i += stride)
+        {
+            const uint64_t k = keys[i];
+            for (int p = 0; p < passes; ++p)
+                atomicAdd(&hist[p * kDigits + static_cast<int>((k >> (shift0 + p * kBits)) & kMask)], 1u);
         }
         __syncthreads();
-        for (int d = threadIdx.x; d < kDigits; d += kThreads)
-            counts[static_cast<size_t>(d) * tiles + blockIdx.x] = hist[d];
+        for (int d = threadIdx.x; d < passes * kDigits; d += kHistThreads)
+            if (hist[d])
+                atomicAdd(&ghist[d], hist[d]);
     }
 
-    __global__ void __launch_bounds__(kThreads, 2) digit_scatter_kernel(
+    __device__ __forceinline__ uint64_t load_relaxed(const uint64_t* p)
+    {
+        uint64_t v;
+        asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+        return v;
+    }
+
+    __device__ __forceinline__ void store_relaxed(uint64_t* p, const uint64_t v)
+    {
+        asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
+    }
+
+    // Exclusive block-wide scan of kPer consecutive values per thread (the thread's digits).
+    __device__ __forceinline__ void block_exclusive(const uint32_t (&v)[kPer], uint32_t (&out)[kPer],
+                                                    uint32_t* __restrict__ warp_sum)
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint32_t mine = 0;
+#pragma unroll
+        for (int q = 0; q < kPer; ++q)
+            mine += v[q];
+        uint32_t incl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o)
+                incl += t;
+        }
+        if (lane == 31)
+            warp_sum[warp] = incl;
+        __syncthreads();
+        uint32_t start = incl - mine;
+        for (int w = 0; w < warp; ++w)
+            start += warp_sum[w];
+#pragma unroll
+        for (int q = 0; q < kPer; ++q)
+        {
+            out[q] = start;
+            start += v[q];
+        }
+    }
+
+    __global__ void __launch_bounds__(kThreads, 3) digit_pass_kernel(
         const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint64_t* __restrict__ keys_out,
-        uint32_t* __restrict__ vals_out, const int n, const int shift, const int tiles,
-        const uint32_t* __restrict__ offsets)
+        uint32_t* __restrict__ vals_out, const int n, const int shift, const int pass,
+        const uint32_t* __restrict__ ghist, uint64_t* __restrict__ status, uint32_t* __restrict__ ticket,
+        unsigned* __restrict__ err)
     {
         extern __shared__ __align__(16) unsigned char smem[];
         uint64_t* stage_k = reinterpret_cast<uint64_t*>(smem);                     // kTile
         uint32_t* stage_v = reinterpret_cast<uint32_t*>(stage_k + kTile);          // kTile
         uint32_t* warp_cnt = stage_v + kTile;                                      // kWarps * kDigits
         uint32_t* digit_start = warp_cnt + kWarps * kDigits;                       // kDigits
-        uint32_t* tile_off = digit_start + kDigits;                                // kDigits
+        uint32_t* gbase = digit_start + kDigits;                                   // kDigits
+        __shared__ uint32_t warp_sum[2][kWarps];
+        __shared__ int tile_s;
 
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (threadIdx.x == 0)
+            tile_s = static_cast<int>(atomicAdd(ticket, 1u));
         for (int d = threadIdx.x; d < kWarps * kDigits; d += kThreads)
             warp_cnt[d] = 0;
-        for (int d = threadIdx.x; d < kDigits; d += kThreads)
-            tile_off[d] = offsets[static_cast<size_t>(d) * tiles + blockIdx.x];
         __syncthreads();
-
-        const int tile_base = blockIdx.x * kTile;
+        const int tile = tile_s;
+        const int tile_base = tile * kTile;
         const int tile_n = min(kTile, n - tile_base);
         const int base = tile_base + warp * (kTile / kWarps);
         const unsigned lt = (1u << lane) - 1u;
-        // only the ranks stay in registers; keys and values are read again (from L1/L2)
-        // when the tile is staged, which keeps the kernel at two CTAs per SM
+
+        // load and rank (out-of-range lanes take digit kDigits, which no key has: they are
+        // matched among themselves, counted nowhere and never written)
+        uint64_t key[kRounds];
         uint32_t rank[kRounds];
 #pragma unroll
         for (int r = 0; r < kRounds; ++r)
         {
             const int i = base + r * 32 + lane;
-            const bool ok = i < n;
-            // out-of-range lanes take a digit value no real key has; they are matched among
-            // themselves, counted nowhere and never written
-            const unsigned d = ok ? static_cast<unsigned>((keys[i] >> shift) & kMask) : static_cast<unsigned>(kDigits);
+            key[r] = i < n ? keys[i] : 0ull;
+        }
+#pragma unroll
+        for (int r = 0; r < kRounds; ++r)
+        {
+            const bool ok = base + r * 32 + lane < n;
+            const unsigned d = ok ? static_cast<unsigned>((key[r] >> shift) & kMask) : static_cast<unsigned>(kDigits);
             const unsigned peers = __match_any_sync(0xffffffffu, d);
             const int leader = __ffs(peers) - 1;
             uint32_t before = 0;
             if (lane == leader && ok)
-            {
-                before = warp_cnt[warp * kDigits + d];
-                warp_cnt[warp * kDigits + d] = before + __popc(peers);
-            }
-            before = __shfl_sync(0xffffffffu, before, leader);
-            rank[r] = before + __popc(peers & lt);
+                before = atomicAdd(&warp_cnt[warp * kDigits + d], static_cast<uint32_t>(__popc(peers)));
+            rank[r] = __shfl_sync(0xffffffffu, before, leader) + __popc(peers & lt);
         }
         __syncthreads();
-        // Thread t owns the consecutive digits kPer*t ..: exclusive scan over warps per digit
-        // (warp_cnt becomes the count in earlier warps) and the digit's total in the tile.
-        constexpr int kPer = kDigits / kThreads;
+
+        // per digit: the count in earlier warps (warp_cnt becomes exclusive over warps) and
+        // the tile's total
         uint32_t total[kPer];
-        uint32_t mine = 0;
 #pragma unroll
         for (int q = 0; q < kPer; ++q)
         {
@@ -125,34 +221,86 @@ namespace nbg
                 run += c;
             }
             total[q] = run;
-            mine += run;
         }
-        // block-wide exclusive scan of the per-thread totals -> where each digit's run starts
-        {
-            __shared__ uint32_t warp_sum[kWarps];
-            uint32_t incl = mine;
+        // publish this tile's counts at once: later tiles may already be waiting for them
+        const uint64_t epoch = static_cast<uint64_t>(pass + 1) << 32;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1)
-            {
-                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o)
-                    incl += v;
-            }
-            if (lane == 31)
-                warp_sum[warp] = incl;
-            __syncthreads();
-            uint32_t before = 0;
-            for (int w = 0; w < warp; ++w)
-                before += warp_sum[w];
-            uint32_t start = before + incl - mine;
+        for (int q = 0; q < kPer; ++q)
+        {
+            const int d = threadIdx.x * kPer + q;
+            store_relaxed(&status[static_cast<size_t>(tile) * kDigits + d],
+                          (tile == 0 ? kFlagInclusive : kFlagAggregate) | epoch | total[q]);
+        }
+        // where each digit starts within the tile, and where it starts in the output
+        {
+            uint32_t start[kPer], gcount[kPer], gstart[kPer];
+            block_exclusive(total, start, warp_sum[0]);
+#pragma unroll
+            for (int q = 0; q < kPer; ++q)
+                gcount[q] = ghist[threadIdx.x * kPer + q];
+            block_exclusive(gcount, gstart, warp_sum[1]);
 #pragma unroll
             for (int q = 0; q < kPer; ++q)
             {
-                digit_start[threadIdx.x * kPer + q] = start;
-                start += total[q];
+                digit_start[threadIdx.x * kPer + q] = start[q];
+                gbase[threadIdx.x * kPer + q] = gstart[q];
+            }
+        }
+        // decoupled look-back: sum the earlier tiles' counts of each digit, four tiles per
+        // step, back to the nearest tile that has published an inclusive count
+        if (tile > 0)
+        {
+#pragma unroll
+            for (int q = 0; q < kPer; ++q)
+            {
+                const int d = threadIdx.x * kPer + q;
+                uint32_t before = 0;
+                int j = tile - 1;
+                uint64_t t0 = 0;
+                while (j >= 0)
+                {
+                    uint64_t w[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        w[u] = j - u >= 0 ? load_relaxed(&status[static_cast<size_t>(j - u) * kDigits + d]) : 0ull;
+                    // take the words in order while they are published aggregates; stop at
+                    // an inclusive one, or wait where one is not published yet
+                    int u = 0;
+                    bool done = false;
+                    for (; u < 4 && j - u >= 0; ++u)
+                    {
+                        if ((w[u] & ~(3ull << 62)) >> 32 != static_cast<uint64_t>(pass + 1) || !(w[u] >> 62))
+                            break;
+                        before += static_cast<uint32_t>(w[u]);
+                        if ((w[u] >> 62) == 2)
+                        {
+                            done = true;
+                            break;
+                        }
+                    }
+                    if (done)
+                        break;
+                    j -= u;
+                    if (j >= 0 && u == 0)
+                    {
+                        // tile j has not published yet: it is running and will
+                        if (!t0)
+                            t0 = globaltimer();
+                        else if (globaltimer() - t0 > kWaitLimitNs)
+                        {
+                            atomicOr(err, DEV_ERR_TIMEOUT);
+                            break;
+                        }
+                        __nanosleep(100);
+                    }
+                }
+                store_relaxed(&status[static_cast<size_t>(tile) * kDigits + d],
+                              kFlagInclusive | epoch | (before + total[q]));
+                gbase[d] += before;
             }
         }
         __syncthreads();
+
         // stage the tile in digit order
 #pragma unroll
         for (int r = 0; r < kRounds; ++r)
@@ -160,64 +308,74 @@ namespace nbg
             const int i = base + r * 32 + lane;
             if (i >= n)
                 continue;
-            const uint64_t key = keys[i];
-            const unsigned d = static_cast<unsigned>((key >> shift) & kMask);
+            const unsigned d = static_cast<unsigned>((key[r] >> shift) & kMask);
             const uint32_t pos = digit_start[d] + warp_cnt[warp * kDigits + d] + rank[r];
-            stage_k[pos] = key;
+            stage_k[pos] = key[r];
             stage_v[pos] = vals[i];
         }
         __syncthreads();
         // write out in staged order: consecutive threads take consecutive staged keys, which
-        // within a digit go to consecutive global positions
+        // within a digit go to consecutive output positions
         for (int s = threadIdx.x; s < tile_n; s += kThreads)
         {
-            const uint64_t key = stage_k[s];
-            const unsigned d = static_cast<unsigned>((key >> shift) & kMask);
-            const uint32_t pos = tile_off[d] + (static_cast<uint32_t>(s) - digit_start[d]);
-            keys_out[pos] = key;
-            vals_out[pos] = stage_v[s];
+            const uint64_t k = stage_k[s];
+            const unsigned d = static_cast<unsigned>((k >> shift) & kMask);
+            const uint32_t pos = gbase[d] + (static_cast<uint32_t>(s) - digit_start[d]);
+            if (pos < static_cast<uint32_t>(n))     // always, unless a look-back wait gave up
+            {
+                keys_out[pos] = k;
+                vals_out[pos] = stage_v[s];
+            }
+            else
+                atomicOr(err, DEV_ERR_BOUNDS);
         }
     }
 
     size_t sort_temp_bytes(const size_t n)
     {
         const size_t tiles = (n + kTile - 1) / kTile;
-        const size_t cnt = tiles * kDigits;
-        return 2 * cnt * sizeof(uint32_t) + scan_temp_elems(cnt) * sizeof(uint32_t) + 256;
+        return zero_bytes(tiles) + 256;
     }
 
     cudaError_t radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt,
                                  const size_t n, const int begin_bit, const int end_bit, void* temp,
-                                 cudaStream_t stream, uint64_t* launches, bool* in_alt)
+                                 cudaStream_t stream, uint64_t* launches, bool* in_alt, unsigned* err)
     {
         *in_alt = false;
         if (n <= 1)
             return cudaSuccess;
+        if (n > 0x7fffffffu)
+            return cudaErrorInvalidValue;
+        const int passes = (end_bit - begin_bit + kBits - 1) / kBits;
+        if (passes < 1 || passes > kMaxPasses)
+            return cudaErrorInvalidValue;
         static const cudaError_t attr = cudaFuncSetAttribute(
-            digit_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kScatterSmem));
+            digit_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kPassSmem));
         if (attr != cudaSuccess)
             return attr;
         const int tiles = static_cast<int>((n + kTile - 1) / kTile);
-        const size_t cnt = static_cast<size_t>(tiles) * kDigits;
-        uint32_t* counts = static_cast<uint32_t*>(temp);
-        uint32_t* offsets = counts + cnt;
-        uint32_t* scan_tmp = offsets + cnt;
+        const TempLayout t = layout(temp, static_cast<size_t>(tiles));
+        cudaError_t e = cudaMemsetAsync(temp, 0, t.zero_bytes, stream);
+        if (e != cudaSuccess)
+            return e;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int hist_grid = std::max(1, std::min((static_cast<int>(n) + kHistThreads - 1) / kHistThreads, 2 * sms));
+        digit_hist_kernel<<<hist_grid, kHistThreads, 0, stream>>>(keys, static_cast<int>(n), begin_bit, passes, t.ghist);
+        ++*launches;
+        e = cudaGetLastError();
+        if (e != cudaSuccess)
+            return e;
         uint64_t* kin = keys;
         uint32_t* vin = vals;
         uint64_t* kout = keys_alt;
         uint32_t* vout = vals_alt;
-        for (int shift = begin_bit; shift < end_bit; shift += kBits)
+        for (int p = 0; p < passes; ++p)
         {
-            digit_count_kernel<<<tiles, kThreads, 0, stream>>>(kin, static_cast<int>(n), shift, tiles, counts);
-            ++*launches;
-            cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess)
-                return e;
-            e = exclusive_scan<uint32_t>(counts, offsets, cnt, scan_tmp, stream, launches);
-            if (e != cudaSuccess)
-                return e;
-            digit_scatter_kernel<<<tiles, kThreads, kScatterSmem, stream>>>(kin, vin, kout, vout, static_cast<int>(n),
-                                                                             shift, tiles, offsets);
+            digit_pass_kernel<<<tiles, kThreads, kPassSmem, stream>>>(kin, vin, kout, vout, static_cast<int>(n),
+                                                                       begin_bit + p * kBits, p, t.ghist + p * kDigits,
+                                                                       t.status, t.tickets + p, err);
             ++*launches;
             e = cudaGetLastError();
             if (e != cudaSuccess)

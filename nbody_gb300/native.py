@@ -36,7 +36,7 @@ EXPORTS = (
     "nbody_cuda_integrate", "nbody_cuda_update", "nbody_cuda_synchronize",
     "nbody_cuda_dev_accel_soa", "nbody_cuda_dev_accel_aos", "nbody_cuda_dev_integrate_soa",
     "nbody_cuda_launch_count", "nbody_cuda_last_direct_config", "nbody_cuda_calibrate_fp32",
-    "nbody_cuda_dev_accel_soa_noalloc", "nbody_cuda_bh_stats", "nbody_cuda_morton",
+    "nbody_cuda_dev_accel_soa_noalloc", "nbody_cuda_bh_stats", "nbody_cuda_bh_stage_ms", "nbody_cuda_morton",
     "nbody_cuda_accel_sampled", "nbody_cuda_split_origin", "nbody_cuda_calibrate_fp64",
     "nbody_cuda_tree_export", "nbody_cuda_set_systems", "nbody_cuda_batch_autotune",
     "nbody_cuda_batch_config_count", "nbody_cuda_batch_config", "nbody_cuda_batch_set_config",
@@ -129,6 +129,7 @@ def lib() -> C.CDLL:
         "nbody_cuda_calibrate_fp32": ([vp, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
         "nbody_cuda_dev_accel_soa_noalloc": ([vp, vp, vp, sz, P, vp], C.c_int),
         "nbody_cuda_bh_stats": ([vp, C.POINTER(C.c_uint64)], C.c_int),
+        "nbody_cuda_bh_stage_ms": ([vp, C.POINTER(C.c_float)], C.c_int),
         "nbody_cuda_morton": ([vp, P, vp, vp, C.POINTER(C.c_double)], C.c_int),
         "nbody_cuda_accel_sampled": ([vp, P, vp, sz, vp], C.c_int),
         "nbody_cuda_split_origin": ([vp, C.POINTER(C.c_double)], C.c_int),
@@ -310,6 +311,12 @@ class Context:
         out = (C.c_uint64 * 3)()
         self.check(lib().nbody_cuda_bh_stats(self.h, out))
         return {"interactions": int(out[0]), "visits": int(out[1]), "cells": int(out[2])}
+
+    def bh_stage_ms(self) -> tuple[float, float]:
+        """(tree build, traversal) device milliseconds of the last Barnes-Hut accelerate."""
+        out = (C.c_float * 2)()
+        self.check(lib().nbody_cuda_bh_stage_ms(self.h, out))
+        return float(out[0]), float(out[1])
 
     def morton(self, p: StepParams):
         n = self.count()

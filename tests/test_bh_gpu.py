@@ -89,6 +89,40 @@ def test_morton_and_sort_order_bit_exact(gpu):
             assert np.array_equal(codes, ref_codes[ref_order])
 
 
+@pytest.mark.parametrize("n", [2, 3, 4095, 4096, 4097, 12289, 1 << 20])
+def test_sort_order_at_tile_edges(gpu, n):
+    """The radix sort (one kernel per digit pass, decoupled look-back between 4096-key
+    tiles) against the oracle's stable order, at sizes on and next to the tile size, with
+    runs of equal codes (ties keep index order)."""
+    rng = np.random.default_rng(n)
+    b = np.zeros((n, 12), np.float32)
+    b[:, :3] = rng.uniform(-30, 30, (n, 3)).astype(np.float32)
+    b[:, 7] = 1.0
+    dup = rng.choice(n, n // 3, replace=True)
+    b[dup, :3] = b[rng.choice(n, 1), :3]        # a third of the bodies share one position
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        codes, order, box = ctx.morton(gpu.params(mode=gpu.MODE_NLOGN, size=0.0, tree_box=1))
+    ref_codes = O.morton63(b[:, :3], box[:3], 2.0 ** 21 / box[3])
+    ref_order = O.sort_order(ref_codes)
+    assert np.array_equal(order, ref_order)
+    assert np.array_equal(codes, ref_codes[ref_order])
+
+
+def test_sort_order_at_16m(gpu):
+    """The sort of the 16.8M disk + halo codes: 4096 tiles per pass, most of them waiting on
+    their predecessors' counts, against the oracle's stable order."""
+    from nbody_gb300 import scenes
+    b = scenes.disk_halo()
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        codes, order, box = ctx.morton(gpu.params(mode=gpu.MODE_NLOGN, size=0.0, tree_box=1))
+    ref_codes = O.morton63(b[:, :3], box[:3], 2.0 ** 21 / box[3])
+    ref_order = O.sort_order(ref_codes)
+    assert np.array_equal(order, ref_order)
+    assert np.array_equal(codes, ref_codes[ref_order])
+
+
 @pytest.mark.parametrize("size,tree_box", [(64.0, 0), (100.0, 0), (0.0, 1)],
                          ids=["pow2-box-integer-path", "other-box-fp64-path", "fitted-box"])
 def test_morton_codes_at_special_values(gpu, size, tree_box):
@@ -286,7 +320,7 @@ def test_tree_export_is_the_reference_tree(gpu, fixture):
     assert np.median(err) <= 1e-5 and (err > TOL).sum() <= len(b) // 500 + 2
 
 
-@pytest.mark.parametrize("per_warp", ["128", "64"])
+@pytest.mark.parametrize("per_warp", ["256", "128", "64"])
 @pytest.mark.parametrize("law", [0, 1], ids=["cutoff", "softened"])
 @pytest.mark.parametrize("n", [1000, 4097, 100000])
 def test_two_targets_per_lane_walk_is_bit_identical(gpu, n, law, per_warp, monkeypatch):
@@ -323,3 +357,24 @@ def test_two_targets_per_lane_walk_is_bit_identical_at_16m(gpu, monkeypatch):
         s32 = ctx.bh_stats()
     assert s64["interactions"] == s32["interactions"]
     assert np.array_equal(a64.view(np.uint32), a32.view(np.uint32))
+
+
+def test_bh_stage_ms(gpu):
+    """nbody_cuda_bh_stage_ms: refused before any Barnes-Hut accelerate; afterwards the build
+    and traversal times are positive and no longer than the whole accelerate."""
+    import time
+    from nbody_gb300 import scenes
+    b = scenes.two_plummer(50000)
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        with pytest.raises(gpu.NbodyError):
+            ctx.bh_stage_ms()
+        p = gpu.params(mode=gpu.MODE_NLOGN, theta=0.5, size=0.0, tree_box=1)
+        ctx.accelerate(p)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.accelerate(p)
+        ctx.synchronize()
+        wall_ms = (time.perf_counter() - t0) * 1e3
+        build, walk = ctx.bh_stage_ms()
+    assert 0 < build and 0 < walk and build + walk <= wall_ms
