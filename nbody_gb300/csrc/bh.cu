@@ -947,13 +947,13 @@ namespace nbg
 #pragma unroll
                 for (int q = 0; q < Q; ++q)
                 {
-                    // bhtree.cpp:117-125, evaluated in the reference's operation order, per
-                    // target, with scalar operations the compiler may not fuse: a packed
-                    // multiply-add chain can be contracted, and one rounding less flips
-                    // borderline acceptances
+                    // bhtree.cpp:117-125, evaluated in the reference's operation order with
+                    // every operation rounded on its own (packed, two targets at a time). A
+                    // contracted multiply-add has one rounding less, which flips borderline
+                    // acceptances; sq2 forms the squares so that none can be contracted.
                     const float2 dx = add2(f2(cm.x), npx[q]), dy = add2(f2(cm.y), npy[q]), dz = add2(f2(cm.z), npz[q]);
-                    const float ds0 = __fadd_rn(__fadd_rn(__fmul_rn(dx.x, dx.x), __fmul_rn(dy.x, dy.x)), __fmul_rn(dz.x, dz.x));
-                    const float ds1 = __fadd_rn(__fadd_rn(__fmul_rn(dx.y, dx.y), __fmul_rn(dy.y, dy.y)), __fmul_rn(dz.y, dz.y));
+                    const float2 ds = add2(add2(sq2(dx), sq2(dy)), sq2(dz));
+                    const float ds0 = ds.x, ds1 = ds.y;
                     take[2 * q] = ((mask[2 * q] >> lane) & 1u) && ds0 > open_r2;
                     take[2 * q + 1] = ((mask[2 * q + 1] >> lane) & 1u) && ds1 > open_r2;
                     if (take[2 * q] || take[2 * q + 1])

@@ -119,5 +119,11 @@ namespace nbg
     __device__ __forceinline__ float2 mul2(const float2 a, const float2 b) { return __fmul2_rn(a, b); }
     __device__ __forceinline__ float2 fma2(const float2 a, const float2 b, const float2 c) { return __ffma2_rn(a, b, c); }
 
+    // The exactly rounded packed square a*a of each half, as a*a + 0 in one FMA. The code
+    // generator fuses a packed multiply into a dependent packed add (one rounding less),
+    // even when both are written as PTX with an explicit .rn; an FMA result cannot be fused
+    // again, and fma(a, a, +0) rounds exactly as the product a*a (a*a is never -0).
+    __device__ __forceinline__ float2 sq2(const float2 a) { return __ffma2_rn(a, a, make_float2(0.f, 0.f)); }
+
     inline unsigned ceil_div(const size_t a, const size_t b) { return static_cast<unsigned>((a + b - 1) / b); }
 }
