@@ -180,8 +180,6 @@ namespace nbg
         const int m_exp = bound_exp(red[6][0]), x_exp = bound_exp(red[7][0]);
         b.mass_shift = 61 - cn - m_exp;
         b.mom_shift = 61 - cn - m_exp - x_exp;
-        b.mass_unit = ldexp(1.0, -b.mass_shift);
-        b.com_unit = ldexp(1.0, x_exp);
         if (mode == 0)
         {
             // tree.h:20 / bhtree.h:29: centred at the origin, edge State::size
@@ -239,6 +237,7 @@ namespace nbg
             b.lo_cells[a] = exact ? static_cast<long long>(lc) : 0;
         }
         b.exact = exact ? 1 : 0;
+        b.edge_f = static_cast<float>(b.edge);
         *box = b;
     }
 
@@ -614,6 +613,17 @@ namespace nbg
         collect_children<DEPTH ? DEPTH - 1 : 0>(ch.x, child, flag, octidx, out, nc, err);
     }
 
+    // An int64 as float: |v| split into two 32-bit halves, each converted exactly or with one
+    // rounding, joined by one FMA (within about an ulp). No FP64 operation: GB300's FP64
+    // pipe is its slowest.
+    __device__ __forceinline__ float i64_to_float(const long long v)
+    {
+        const unsigned long long u = v < 0 ? 0ull - static_cast<unsigned long long>(v) : static_cast<unsigned long long>(v);
+        const float f = fmaf(static_cast<float>(static_cast<uint32_t>(u >> 32)), 4294967296.0f,
+                             static_cast<float>(static_cast<uint32_t>(u)));
+        return v < 0 ? -f : f;
+    }
+
     // latency bound (chains of dependent loads): full occupancy, 32 registers
     __global__ void __launch_bounds__(256, 7) octnode_kernel(const int2* __restrict__ child, const int2* __restrict__ range,
                                    const int* __restrict__ prefix, const uint32_t* __restrict__ flag,
@@ -635,17 +645,20 @@ namespace nbg
         OctNode* out = nodes + octidx[i];
         if (ms > 0)
         {
-            // com = (sum of m x 2^mom_shift) / (sum of m 2^mass_shift) * 2^(mass_shift - mom_shift)
-            const double inv = box->com_unit / static_cast<double>(ms);
-            out->com_mass = make_float4(static_cast<float>(static_cast<double>(hi.x - lo.x) * inv),
-                                        static_cast<float>(static_cast<double>(hi.y - lo.y) * inv),
-                                        static_cast<float>(static_cast<double>(hi.z - lo.z) * inv),
-                                        static_cast<float>(static_cast<double>(ms) * box->mass_unit));
+            // com = (sum of m x 2^mom_shift) / (sum of m 2^mass_shift) * 2^(mass_shift - mom_shift),
+            // in float: the quotient lies in [-1, 1] before the exact power-of-two scaling
+            const int shift = box->mass_shift - box->mom_shift;
+            const float fm = i64_to_float(ms);
+            const float rm = __frcp_rn(fm);
+            out->com_mass = make_float4(ldexpf(i64_to_float(hi.x - lo.x) * rm, shift),
+                                        ldexpf(i64_to_float(hi.y - lo.y) * rm, shift),
+                                        ldexpf(i64_to_float(hi.z - lo.z) * rm, shift),
+                                        ldexpf(fm, -box->mass_shift));
         }
         else
             out->com_mass = make_float4(0.f, 0.f, 0.f, 0.f);
         // the reference's node size is the root size halved per level, in float
-        const float sz = static_cast<float>(ldexp(box->edge, -lvl));
+        const float sz = ldexpf(box->edge_f, -lvl);
         const float open_r2 = __fmul_rn(__fmul_rn(sz, sz), __fmul_rn(theta, theta));
         int4* kids = reinterpret_cast<int4*>(out->child);
         kids[0] = make_int4(0, 0, 0, 0);

@@ -28,8 +28,7 @@ namespace nbg
         // bodies below 2^61 (from the largest finite |m| and |x|, see box_final_kernel).
         int mass_shift;
         int mom_shift;
-        double mass_unit;   // 2^-mass_shift: the mass of one fixed-point unit
-        double com_unit;    // 2^(mass_shift - mom_shift): moment units per mass unit
+        float edge_f;       // the edge in float (exact: a float size or a power of two)
     };
 
     // One octree cell: 64 bytes, read whole by a warp (a broadcast load per field).

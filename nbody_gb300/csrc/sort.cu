@@ -13,12 +13,12 @@
 // already running and that publish their counts before they wait themselves, so the wait
 // always ends; it is still bounded in time, and a wait that gives up records
 // DEV_ERR_TIMEOUT. Counts are exact integers, so the result does not depend on timing.
-// Stability: warp w of a CTA owns the contiguous slice [w*512, (w+1)*512) of the tile and
-// walks it in 16 rounds of 32 consecutive keys; a key's rank is (equal digits in earlier
+// Stability: warp w of a CTA owns the contiguous slice [w*256, (w+1)*256) of the tile and
+// walks it in 8 rounds of 32 consecutive keys; a key's rank is (equal digits in earlier
 // warps) + (equal digits in earlier rounds of its warp) + (equal digits on lower lanes of
-// its round, from __match_any_sync). A round's per-warp count is taken and advanced by one
-// shared-memory atomic of the round's leader lane; a warp's atomics complete in program
-// order, so rounds count in order. Equal keys therefore keep their input order, and a
+// its round, from __match_any_sync). A round's per-warp count (16 bits, two to a word) is
+// taken and advanced by one shared-memory atomic of the round's leader lane; a warp's
+// atomics complete in program order, so rounds count in order. Equal keys therefore keep their input order, and a
 // sort of (code, index) pairs starting from index order yields the order by (code, index).
 #include <algorithm>
 
@@ -29,9 +29,9 @@ namespace nbg
 {
     namespace
     {
-        constexpr int kThreads = 256;
+        constexpr int kThreads = 512;
         constexpr int kWarps = kThreads / 32;
-        constexpr int kRounds = 16;
+        constexpr int kRounds = 8;
         constexpr int kTile = kThreads * kRounds;     // 4096 keys per CTA
         constexpr int kBits = 9;
         constexpr int kDigits = 1 << kBits;
@@ -46,10 +46,10 @@ namespace nbg
         constexpr uint64_t kFlagAggregate = 1ull << 62;    // this tile's own count
         constexpr uint64_t kFlagInclusive = 2ull << 62;    // count of this and all earlier tiles
 
-        // dynamic shared memory of a pass: staged keys and values, per-warp counters, digit
-        // starts within the tile and global digit bases
+        // dynamic shared memory of a pass: staged keys and values, per-warp 16-bit counters,
+        // digit starts within the tile and global digit bases (68 KB: three CTAs per SM)
         constexpr size_t kPassSmem = sizeof(uint64_t) * kTile + sizeof(uint32_t) * kTile
-                                     + sizeof(uint32_t) * (kWarps * kDigits + 2 * kDigits);
+                                     + sizeof(uint16_t) * kWarps * kDigits + sizeof(uint32_t) * 2 * kDigits;
 
         struct TempLayout
         {
@@ -163,8 +163,9 @@ namespace nbg
         extern __shared__ __align__(16) unsigned char smem[];
         uint64_t* stage_k = reinterpret_cast<uint64_t*>(smem);                     // kTile
         uint32_t* stage_v = reinterpret_cast<uint32_t*>(stage_k + kTile);          // kTile
-        uint32_t* warp_cnt = stage_v + kTile;                                      // kWarps * kDigits
-        uint32_t* digit_start = warp_cnt + kWarps * kDigits;                       // kDigits
+        uint32_t* warp_cnt2 = stage_v + kTile;                                     // kWarps * kDigits / 2
+        uint16_t* warp_cnt = reinterpret_cast<uint16_t*>(warp_cnt2);               // kWarps * kDigits
+        uint32_t* digit_start = warp_cnt2 + kWarps * kDigits / 2;                  // kDigits
         uint32_t* gbase = digit_start + kDigits;                                   // kDigits
         __shared__ uint32_t warp_sum[2][kWarps];
         __shared__ int tile_s;
@@ -172,8 +173,8 @@ namespace nbg
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         if (threadIdx.x == 0)
             tile_s = static_cast<int>(atomicAdd(ticket, 1u));
-        for (int d = threadIdx.x; d < kWarps * kDigits; d += kThreads)
-            warp_cnt[d] = 0;
+        for (int d = threadIdx.x; d < kWarps * kDigits / 2; d += kThreads)
+            warp_cnt2[d] = 0;
         __syncthreads();
         const int tile = tile_s;
         const int tile_base = tile * kTile;
@@ -200,7 +201,13 @@ namespace nbg
             const int leader = __ffs(peers) - 1;
             uint32_t before = 0;
             if (lane == leader && ok)
-                before = atomicAdd(&warp_cnt[warp * kDigits + d], static_cast<uint32_t>(__popc(peers)));
+            {
+                // counter warp * kDigits + d is the (d & 1) half of word (warp * kDigits + d) / 2
+                const unsigned half = (d & 1u) * 16u;
+                const uint32_t old = atomicAdd(&warp_cnt2[(warp * kDigits + static_cast<int>(d)) >> 1],
+                                               static_cast<uint32_t>(__popc(peers)) << half);
+                before = (old >> half) & 0xffffu;
+            }
             rank[r] = __shfl_sync(0xffffffffu, before, leader) + __popc(peers & lt);
         }
         __syncthreads();
@@ -217,7 +224,7 @@ namespace nbg
             for (int w = 0; w < kWarps; ++w)
             {
                 const uint32_t c = warp_cnt[w * kDigits + d];
-                warp_cnt[w * kDigits + d] = run;
+                warp_cnt[w * kDigits + d] = static_cast<uint16_t>(run);    // < kTile
                 run += c;
             }
             total[q] = run;
