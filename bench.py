@@ -27,7 +27,9 @@ Printed JSON line (rank 0):
                   and the traversal's interactions (20 flop each) against the FFMA peak.
                   Its "transfer" object times the host transfer paths (staged, mapped,
                   direct) for all 16.8M Body records against the copy engine's pinned
-                  bandwidth, and one frame of update + state().
+                  bandwidth, and one frame of update + state(). Its "cpu_reference_bh"
+                  object times one full step of the restated CPU Barnes-Hut on the same
+                  bodies on all host cores.
   configs         configs 1 (N = 4096 Plummer, 100 steps) and 2 (2 x 131072 Plummer BH).
   scene_generators util::disk and util::cube on the device at N = 16,777,216, against the
                   reference's serial generator on 1,048,576 bodies.
@@ -453,6 +455,17 @@ def bench_bh16m(torch, stream, flush, native, scenes, args):
         p = native.params(mode=native.MODE_NLOGN, theta=0.5, law=native.LAW_SOFTENED, eps2=0.005 ** 2,
                           dt=2.5e-4, size=0.0, tree_box=1, precision=native.PREC_COMPENSATED)
         res["transfer"] = bench_transfer(torch, native, ctx, b, p)
+    # one full step of the restated CPU Barnes-Hut on the same bodies, on all host cores:
+    # the reference's fixed root box (centred at the origin), made a power of two that holds
+    # every body
+    size = float(2.0 ** np.ceil(np.log2(2.0 * float(np.abs(b[:, :3]).max()))))
+    cpu_s, cores = cpu_barnes_hut_rate(b, size, 0.5)
+    res["cpu_reference_bh"] = {
+        "theta": 0.5, "step_s": cpu_s, "cores": cores, "body_steps_per_s": n / cpu_s,
+        "kind": "port (restated CpuBarnesHutSolver, cpu_barnes_hut.h:22-44: serial tree build, "
+                "parallel traversal)",
+        "root_box": f"centred at the origin, edge {size:g}",
+        "gpu_speedup": cpu_s / (res["theta_0.5"]["ms_per_step"] * 1e-3)}
     return res
 
 
