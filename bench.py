@@ -69,9 +69,9 @@ WORKLOAD = ("direct-sum step, N=1048576 uniform unit cube at rest, log-normal(0,
 FLOP_PER_PAIR = 20
 N_SAMPLE = 65536
 # ncu DRAM bytes (read + write) of one N = 2^20 direct-sum launch, by (targets per thread,
-# block, jsplit): the j-split partials stay mostly in L2, so traffic is far below the
-# 16 MB x (1 + jsplit) the launch touches.
-MEASURED_TRAFFIC = {(4, 256, 4): 17975296 + 11777024}
+# block, packed mode, jsplit): the j-split partials stay mostly in L2, so traffic is far
+# below the 16 MB x (1 + jsplit) the launch touches.
+MEASURED_TRAFFIC = {(4, 256, 1, 4): 17975296 + 11777024, (4, 256, 2, 4): 18174976 + 12430080}
 
 
 def env_rank():
@@ -323,7 +323,9 @@ def _bench_gpu(args, stream):
                          "peak_scalar_ffma": s_tf, "peak_packed_ffma2": p_tf,
                          "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs,
                          "kernel_ms": acc_ms,
-                         "traffic": MEASURED_TRAFFIC.get((cfg["targets_per_thread"], cfg["block"], cfg["jsplit"])),
+                         "traffic": MEASURED_TRAFFIC.get((cfg["targets_per_thread"], cfg["block"],
+                                                          native.Context.direct_variant(tuned)["packed"],
+                                                          cfg["jsplit"])),
                          "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one N=2^20 launch of the "
                                          "chosen shape (profiles/direct_fp32_n262144_full.md); null for a shape "
                                          "not captured"},

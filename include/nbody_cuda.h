@@ -336,8 +336,9 @@ int nbody_cuda_tree_query(nbody_cuda* ctx, const void* nodes, size_t count, cons
 /* --- direct-sum kernel shapes ---------------------------------------------------------------- */
 
 /* Number of instantiated direct-sum kernel shapes; describe one (targets per thread, threads
- * per CTA, packed FP32x2 arithmetic or scalar); pin one for this context (index < 0 returns
- * to the size-based choice). */
+ * per CTA, *packed: 0 scalar FP32, 1 packed FP32x2, 2 packed with each source tile first
+ * rewritten as ready-made operand pairs); pin one for this context (index < 0 returns to the
+ * size-based choice). */
 int nbody_cuda_direct_variant_count(void);
 int nbody_cuda_direct_variant(int index, int* targets_per_thread, int* block, int* packed);
 int nbody_cuda_set_direct_variant(nbody_cuda* ctx, int index);

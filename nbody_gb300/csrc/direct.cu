@@ -13,7 +13,9 @@
 //     3 FADD2 + 3 FFMA2 + 2 MUFU.RSQ + 3 FMUL2 + 3 FFMA2 for two targets.
 //   - sources stream through shared memory in TILE-body tiles, STAGES deep, each tile
 //     one TMA bulk copy (cp.async.bulk) completing on an mbarrier; every thread reads
-//     the same source (a broadcast shared load) and applies it to its T targets.
+//     the same source (a broadcast shared load) and applies it to its T targets. In the
+//     pre-paired shapes (DUP) each landed tile is first rewritten once as operand pairs
+//     {x,x,y,y}, {z,z,m,m}, which the inner loop reads with two 16-byte loads.
 //   - the source range can be split into `jsplit` chunks (blockIdx.y) so that the grid
 //     fills the 152 SMs evenly; chunk partials go to a scratch array and are summed in
 //     a fixed order (deterministic) by reduce_partials or the fused integrate.
@@ -97,7 +99,10 @@ namespace nbg
         static constexpr int kRec = AOS ? 3 : 1;
     };
 
-    template <int T, int BLOCK, int TILE, int STAGES, int LAW, bool AOS, bool PACKED = true>
+    // DUP: each landed tile is first rewritten in shared memory as source pairs {x,x,y,y},
+    // {z,z,m,m}, so the inner loop reads the packed operands ready-made (two 16-byte loads)
+    // instead of broadcasting each scalar into a register pair.
+    template <int T, int BLOCK, int TILE, int STAGES, int LAW, bool AOS, bool PACKED = true, bool DUP = false>
     __global__ void __launch_bounds__(BLOCK, (T >= 8 ? 2 : 3))
     direct_fp32_kernel(const float4* __restrict__ src,        // pos_mass (SoA) or Body (AoS)
                        const float4* __restrict__ vel_radius, // SoA radius source (CUTOFF)
@@ -109,6 +114,7 @@ namespace nbg
         constexpr int P = T / 2;
         constexpr int REC = Layout<AOS>::kRec;
         __shared__ __align__(128) float4 tile[STAGES][TILE * REC];
+        __shared__ __align__(16) float4 pairs[DUP ? 2 * TILE : 1];
         __shared__ __align__(8) uint64_t bar[STAGES];
 
         const int tid = threadIdx.x;
@@ -185,15 +191,39 @@ namespace nbg
                 __syncthreads();
             }
             const float4* tl = tile[stage];
-#pragma unroll 2
-            for (int j = 0; j < TILE; ++j)
+            if (DUP)
             {
-                const float4 s = tl[j * REC];
-                const float m = AOS ? tl[j * REC + 1].w : s.w;
-                const float2 sx = f2(s.x), sy = f2(s.y), sz = f2(s.z), sm = f2(m);
+                for (int j = tid; j < TILE; j += BLOCK)
+                {
+                    const float4 s = tl[j * REC];
+                    const float m = AOS ? tl[j * REC + 1].w : s.w;
+                    pairs[2 * j] = make_float4(s.x, s.x, s.y, s.y);
+                    pairs[2 * j + 1] = make_float4(s.z, s.z, m, m);
+                }
+                __syncthreads();
+#pragma unroll 2
+                for (int j = 0; j < TILE; ++j)
+                {
+                    const float4 a = pairs[2 * j], b = pairs[2 * j + 1];
+                    const float2 sx = make_float2(a.x, a.y), sy = make_float2(a.z, a.w);
+                    const float2 sz = make_float2(b.x, b.y), sm = make_float2(b.z, b.w);
 #pragma unroll
-                for (int p = 0; p < P; ++p)
-                    interact2<LAW, PACKED>(sx, sy, sz, sm, nx[p], ny[p], nz[p], lim[p], ax[p], ay[p], az[p]);
+                    for (int p = 0; p < P; ++p)
+                        interact2<LAW, PACKED>(sx, sy, sz, sm, nx[p], ny[p], nz[p], lim[p], ax[p], ay[p], az[p]);
+                }
+            }
+            else
+            {
+#pragma unroll 2
+                for (int j = 0; j < TILE; ++j)
+                {
+                    const float4 s = tl[j * REC];
+                    const float m = AOS ? tl[j * REC + 1].w : s.w;
+                    const float2 sx = f2(s.x), sy = f2(s.y), sz = f2(s.z), sm = f2(m);
+#pragma unroll
+                    for (int p = 0; p < P; ++p)
+                        interact2<LAW, PACKED>(sx, sy, sz, sm, nx[p], ny[p], nz[p], lim[p], ax[p], ay[p], az[p]);
+                }
             }
             __syncthreads();
             if (tid == 0 && t + STAGES < ntiles)
@@ -278,23 +308,24 @@ namespace nbg
         struct Variant
         {
             int T, block;
-            bool packed;
+            bool packed, dup;
             KernelFn fn[2][2];  // [law][aos]
         };
 
-        constexpr int kPlanned = 4;
+        constexpr int kPlanned = 3;
 
-        template <int T, int B, bool PACKED = true>
+        template <int T, int B, bool PACKED = true, bool DUP = false>
         Variant make_variant()
         {
             Variant v;
             v.T = T;
             v.block = B;
             v.packed = PACKED;
-            v.fn[0][0] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_CUTOFF, false, PACKED>;
-            v.fn[0][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_CUTOFF, true, PACKED>;
-            v.fn[1][0] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, false, PACKED>;
-            v.fn[1][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, true, PACKED>;
+            v.dup = DUP;
+            v.fn[0][0] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_CUTOFF, false, PACKED, DUP>;
+            v.fn[0][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_CUTOFF, true, PACKED, DUP>;
+            v.fn[1][0] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, false, PACKED, DUP>;
+            v.fn[1][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, true, PACKED, DUP>;
             return v;
         }
 
@@ -303,14 +334,16 @@ namespace nbg
             // The first kPlanned entries are what plan_direct chooses between by size; the
             // rest are further shapes the direct-sum autotuner can time and pin.
             static const Variant v[] = {
+                make_variant<4, 256, true, true>(),     // the fastest at N >= 65536 (timed)
+                make_variant<4, 128>(),
+                make_variant<2, 64>(),                  // the fastest at N = 16384
                 make_variant<8, 256>(),
                 make_variant<4, 256>(),
-                make_variant<4, 128>(),
-                make_variant<2, 64>(),
                 make_variant<8, 256, false>(),
                 make_variant<8, 128>(),
                 make_variant<6, 128>(),
                 make_variant<12, 128>(),
+                make_variant<8, 256, true, true>(),
             };
             *count = static_cast<int>(sizeof(v) / sizeof(v[0]));
             return v;
@@ -440,7 +473,7 @@ namespace nbg
         const Variant* vs = variants(&nv);
         *T = vs[i].T;
         *block = vs[i].block;
-        *packed = vs[i].packed ? 1 : 0;
+        *packed = vs[i].dup ? 2 : (vs[i].packed ? 1 : 0);
     }
 
     cudaError_t launch_reduce(const float4* scratch, const int jsplit, const int n, float4* acc,

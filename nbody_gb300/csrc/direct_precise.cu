@@ -195,6 +195,8 @@ namespace nbg
     {
         constexpr int P = T / 2;
         __shared__ __align__(128) float4 tile[kStages][kTileC];
+        // each landed tile rewritten as operand pairs {x,x,y,y}, {z,z,m,m} (see direct.cu)
+        __shared__ __align__(16) float4 pairs[2 * kTileC];
         __shared__ __align__(8) uint64_t bar[kStages];
         const int tid = threadIdx.x;
         const int base = blockIdx.x * (BLOCK * T);
@@ -262,13 +264,21 @@ namespace nbg
                 __syncthreads();
             }
             const float4* tl = tile[stage];
+            for (int j = tid; j < kTileC; j += BLOCK)
+            {
+                const float4 s = tl[j];
+                pairs[2 * j] = make_float4(s.x, s.x, s.y, s.y);
+                pairs[2 * j + 1] = make_float4(s.z, s.z, s.w, s.w);
+            }
+            __syncthreads();
             for (int sb = 0; sb < kTileC; sb += kSub)
             {
 #pragma unroll 2
                 for (int j = sb; j < sb + kSub; ++j)
                 {
-                    const float4 s = tl[j];
-                    const float2 sx = f2(s.x), sy = f2(s.y), sz = f2(s.z), sm = f2(s.w);
+                    const float4 a = pairs[2 * j], b = pairs[2 * j + 1];
+                    const float2 sx = make_float2(a.x, a.y), sy = make_float2(a.z, a.w);
+                    const float2 sz = make_float2(b.x, b.y), sm = make_float2(b.z, b.w);
 #pragma unroll
                     for (int p = 0; p < P; ++p)
                         interact2c<LAW>(sx, sy, sz, sm, nx[p], ny[p], nz[p], lim[p], ax[p], ay[p], az[p]);

@@ -368,6 +368,10 @@ class Context:
             raise NbodyError(st, f"no direct-sum kernel shape {index}")
         return dict(zip(("targets_per_thread", "block", "packed"), (x.value for x in v)))
 
+    @staticmethod
+    def direct_variant_count() -> int:
+        return int(lib().nbody_cuda_direct_variant_count())
+
     def set_direct_variant(self, index: int):
         self.check(lib().nbody_cuda_set_direct_variant(self.h, index))
 

@@ -268,3 +268,30 @@ def test_caller_owned_device_buffers(gpu):
         bb[:, 8:11] = ref
         expect = O.integrate(bb, 0.5, 10000.0, False)
         assert np.array_equal(pm.cpu().numpy()[:, :3], expect[:, :3])
+
+
+@pytest.mark.parametrize("layout", [0, 1], ids=["soa", "aos"])
+@pytest.mark.parametrize("law", [0, 1], ids=["cutoff", "softened"])
+def test_every_kernel_shape(gpu, law, layout):
+    """Each instantiated direct-sum shape (the ones the autotuner may pin: targets per
+    thread x threads, scalar, packed, and packed with pre-paired source tiles), pinned in
+    turn, on a ragged size whose launch splits the sources: within the direct-sum
+    tolerance of the FP64 oracle, and each repeats exactly."""
+    from nbody_gb300 import scenes
+    n = 9001
+    b = scenes.uniform_cube(n, seed=77)
+    b[:, 3] = np.float32(1e-3)                       # target radius for the cutoff law
+    eps2 = 1e-6 if law == gpu.LAW_SOFTENED else 0.0
+    p = gpu.params(law=law, eps2=eps2)
+    count = gpu.Context.direct_variant_count()
+    assert count >= 10
+    with gpu.Context(layout) as ctx:
+        ctx.upload_bodies(b)
+        for i in range(count):
+            ctx.set_direct_variant(i)
+            ctx.accelerate(p)
+            out = ctx.download_bodies()[:, 8:11].copy()
+            ctx.accelerate(p)
+            assert np.array_equal(out, ctx.download_bodies()[:, 8:11]), gpu.Context.direct_variant(i)
+            err = scaled_err(out, b, law, eps2=eps2)
+            assert err.max() <= TOL_MAX and np.median(err) <= TOL_MEDIAN, (gpu.Context.direct_variant(i), err.max())
