@@ -378,3 +378,37 @@ def test_bh_stage_ms(gpu):
         wall_ms = (time.perf_counter() - t0) * 1e3
         build, walk = ctx.bh_stage_ms()
     assert 0 < build and 0 < walk and build + walk <= wall_ms
+
+
+@pytest.mark.parametrize("tree_box", [1, 0], ids=["fitted-box", "reference-box"])
+def test_bh_wide_mass_range_and_outlier(gpu, tree_box):
+    """Masses over twelve decades, a body far outside the cluster and massless bodies: the
+    cell sums' fixed-point scale comes from the largest |m| and |x|. The GPU tree's force
+    error against an FP64 direct sum is no worse than the reference Barnes-Hut's own at the
+    same theta (the oracle's restated octree, built on the same root box)."""
+    from nbody_gb300 import scenes
+    b = scenes.two_plummer(10000).copy()
+    rng = np.random.default_rng(12)
+    b[:, 7] = (10.0 ** rng.uniform(-8, 4, len(b))).astype(np.float32)
+    b[:40, 7] = 0.0                                 # massless bodies
+    b[5, :3] = (3000.0, -2000.0, 1500.0)            # far outside the cluster
+    size = 8192.0
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        p = gpu.params(mode=gpu.MODE_NLOGN, theta=0.5, law=gpu.LAW_CUTOFF, size=size, tree_box=tree_box)
+        _, _, box = ctx.morton(p)
+        ctx.accelerate(p)
+        acc = ctx.download_bodies()[:, 8:11].astype(np.float64)
+    assert np.all(np.isfinite(acc))
+    tg = rng.choice(len(b), 2048, replace=False)
+    a64 = O.direct_f64(b[:, [0, 1, 2, 7]], 1.0, 0.0, O.LAW_CUTOFF, radius=b[:, 3], targets=tg)
+    # the reference's octree on the same root box (bhtree.cpp:14-85, body by body)
+    t = O.Tree(float(box[3]), center=box[:3] + 0.5 * box[3])
+    for row in b:
+        t.insert(row[:3], row[7])
+    ref, _ = t.accel(b, 0.5, 1.0, targets=tg)
+    mag = np.maximum(np.linalg.norm(a64, axis=1), 1e-30)
+    err_gpu = np.linalg.norm(acc[tg] - a64, axis=1) / mag
+    err_ref = np.linalg.norm(ref - a64, axis=1) / mag
+    assert np.median(err_gpu) <= 1.05 * np.median(err_ref) + 1e-7, (np.median(err_gpu), np.median(err_ref))
+    assert np.percentile(err_gpu, 99) <= 1.5 * np.percentile(err_ref, 99) + 1e-6
