@@ -3,13 +3,15 @@
 //
 // Pipeline per accelerate (all on the context's stream, no host round trip):
 //   1. root box: the reference's fixed box centred at the origin with edge State::size
-//      (source/detail/tree.h:20), or the smallest power-of-two cube around the FP64
-//      bounding box of the bodies (tree_box = 1);
-//   2. morton_kernel: 21 bits per axis, q = floor((x - lo) * 2^21 / edge) with both
-//      double operations rounded toward -inf, clamped, interleaved x -> bit 0. For a
-//      power-of-two box with an exact corner this puts every body in exactly the octant
-//      the reference's float centre comparisons choose (bounds.h:31-38), whose octant
-//      bit is set when the coordinate is below the centre: reference octant = digit ^ 7.
+//      (source/detail/tree.h:20), or the smallest power-of-two cube around the bodies'
+//      bounding box (tree_box = 1; an exact FP32 min/max); the same pass finds the
+//      largest |m| and |x|, which fix the fixed-point scale of step 4;
+//   2. morton_kernel: 21 bits per axis, q = floor((x - lo) * 2^21 / edge), clamped and
+//      interleaved x -> bit 0: in integers for power-of-two cells on a cell-aligned corner
+//      (always for the fitted box), else with both double operations rounded toward
+//      -inf. Either way every body lands in exactly the octant the reference's float
+//      centre comparisons choose (bounds.h:31-38), whose octant bit is set when the
+//      coordinate is below the centre: reference octant = digit ^ 7;
 //   3. radix_sort_pairs over (code, index): stable, so ties keep index order;
 //   4. gather_kernel + cell_sum_kernel: bodies into Morton order, and exact fixed-point
 //      (int64) prefix sums of m and m*x, whose differences give each cell's mass and COM;
@@ -23,12 +25,15 @@
 //      as its deepest cell: that is the node kept. Each node lists its <= 8 children
 //      (cells or single bodies); cells at the Morton limit (identical codes) are buckets
 //      whose bodies are applied one by one when opened;
-//   7. traverse_kernel: a warp walks the tree for 32 Morton-consecutive targets with one
-//      shared stack of (node, lane mask) entries. Every lane evaluates the reference test
-//      itself -- accept when |com - x|^2 > size^2 * theta^2 (bhtree.cpp:117-125), leaves
-//      always applied, massless nodes skipped -- and a node is opened only for the lanes
-//      that rejected it, so each target sums exactly the nodes the reference's traversal
-//      would, in a different order.
+//   7. traverse_pairs_kernel (the default; traverse_kernel is its one-target-per-lane
+//      form): a warp walks the tree for 128 Morton-consecutive targets, four per lane as
+//      two packed pairs, with one shared stack of (node, lane mask per target slot)
+//      entries. Every target evaluates the reference test itself -- accept when
+//      |com - x|^2 > size^2 * theta^2 (bhtree.cpp:117-125), leaves always applied,
+//      massless nodes skipped -- and a node is opened only for the targets that rejected
+//      it, so each target sums exactly the nodes the reference's traversal would, in a
+//      different order (the same order in every walk width, so the sums agree bit for
+//      bit).
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
