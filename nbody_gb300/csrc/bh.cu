@@ -82,7 +82,8 @@ namespace nbg
         size_t temp_bytes = 0;
         BoxParams* box = nullptr;
         double* bbox_part = nullptr;
-        unsigned long long* stats = nullptr;   // [0] interactions, [1] node visits, [2] octree nodes
+        unsigned long long* stats = nullptr;   // [0] interactions, [1] node visits, [2] octree nodes,
+                                               // [3] the traversal's tile counter
         const uint32_t* order = nullptr;       // sorted indices of the last build (keys/vals ping-pong)
         const uint64_t* codes = nullptr;
         bool built = false;                    // a tree for built_n bodies is on the device
@@ -715,7 +716,15 @@ namespace nbg
         const unsigned lt = (1u << lane) - 1u;
         unsigned inter = 0, visits = 0;
 
-        for (int tile = blockIdx.x * kTravWarps + warp; tile * 32 < n; tile += gridDim.x * kTravWarps)
+        // 32-target tiles are handed out in order by a counter (stats[3], zeroed with the
+        // statistics at every build), so warps that drew cheap tiles take more of them
+        auto next_tile = [&]() {
+            unsigned long long t = 0;
+            if (lane == 0)
+                t = atomicAdd(&stats[3], 1ull);
+            return static_cast<int>(__shfl_sync(0xffffffffu, t, 0));
+        };
+        for (int tile = next_tile(); static_cast<long long>(tile) * 32 < n; tile = next_tile())
         {
             const int k = tile * 32 + lane;
             const bool valid = k < n;
@@ -890,7 +899,16 @@ namespace nbg
         const unsigned lt = (1u << lane) - 1u;
         unsigned inter = 0, visits = 0;
 
-        for (int tile = blockIdx.x * W + warp; tile * TW < n; tile += gridDim.x * W)
+        // tiles are handed out in order by a counter (stats[3], zeroed with the statistics at
+        // every build), so warps that drew cheap tiles take more of them: a tile from the
+        // dense centre of a disk costs many times one from its edge
+        auto next_tile = [&]() {
+            unsigned long long t = 0;
+            if (lane == 0)
+                t = atomicAdd(&stats[3], 1ull);
+            return static_cast<int>(__shfl_sync(0xffffffffu, t, 0));
+        };
+        for (int tile = next_tile(); static_cast<long long>(tile) * TW < n; tile = next_tile())
         {
             float2 npx[Q], npy[Q], npz[Q], lim[Q], ax[Q], ay[Q], az[Q];
             unsigned m0[H];
@@ -1302,8 +1320,7 @@ namespace nbg
                 fn = soft ? traverse_pairs_kernel<NBODY_LAW_SOFTENED, 2> : traverse_pairs_kernel<NBODY_LAW_CUTOFF, 2>;
             else
                 fn = soft ? traverse_pairs_kernel<NBODY_LAW_SOFTENED, 1> : traverse_pairs_kernel<NBODY_LAW_CUTOFF, 1>;
-            // one resident wave of CTAs: the grid-stride loop gives every CTA the same number
-            // of tiles, so a second, partial wave would leave most SMs idle
+            // one resident wave of CTAs, each warp drawing tiles until none are left
             int per = 0;
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, warps * 32, 0) != cudaSuccess || per < 1)
                 per = 1;
