@@ -412,3 +412,46 @@ def test_bh_wide_mass_range_and_outlier(gpu, tree_box):
     err_ref = np.linalg.norm(ref - a64, axis=1) / mag
     assert np.median(err_gpu) <= 1.05 * np.median(err_ref) + 1e-7, (np.median(err_gpu), np.median(err_ref))
     assert np.percentile(err_gpu, 99) <= 1.5 * np.percentile(err_ref, 99) + 1e-6
+
+
+def oracle_bh_on_box(bodies, box, theta, targets=None):
+    """The reference's octree (bhtree.cpp:14-138, restated) built body by body on the given
+    root box (lower corner xyz, edge), and its accelerations."""
+    t = O.Tree(float(box[3]), center=np.asarray(box[:3]) + 0.5 * box[3])
+    for row in bodies:
+        t.insert(row[:3], row[7])
+    acc, inter = t.accel(bodies, theta, 1.0, targets=targets)
+    return acc.astype(np.float64), inter
+
+
+@pytest.mark.parametrize("n", [2, 3, 5, 33, 4097])
+def test_bh_small_sizes_fitted_box(gpu, n):
+    """Tiny systems on the fitted power-of-two box (tree_box = 1), against the reference's
+    octree on the same box."""
+    from nbody_gb300 import scenes
+    b = scenes.plummer(n, seed=50 + n, rmax=10.0)
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        p = gpu.params(mode=gpu.MODE_NLOGN, theta=0.5, size=0.0, tree_box=1)
+        _, _, box = ctx.morton(p)
+        ctx.accelerate(p)
+        acc = ctx.download_bodies()[:, 8:11]
+    ref, _ = oracle_bh_on_box(b, box, 0.5)
+    err = np.linalg.norm(acc - ref, axis=1) / term_scale(b)
+    assert np.all(np.isfinite(acc)) and err.max() <= TOL
+
+
+@pytest.mark.parametrize("tree_box", [1, 0], ids=["fitted-box", "reference-box"])
+@pytest.mark.parametrize("law", [0, 1], ids=["cutoff", "softened"])
+def test_bh_all_bodies_at_one_point(gpu, law, tree_box):
+    """Every body at the same position: a zero-extent bounding box and one bucket of
+    identical codes. Each pair has d = 0, which the cutoff removes and the softened law
+    multiplies out, so every acceleration is exactly zero, as in the reference."""
+    n = 100
+    b = np.zeros((n, 12), np.float32)
+    b[:, :3] = (1.5, -2.25, 0.75)
+    b[:, 3] = 0.01
+    b[:, 7] = 1.0
+    acc, stats = bh_accel(gpu, b, theta=0.5, law=law, eps2=1e-4 if law == 1 else 0.0, size=64.0, tree_box=tree_box)
+    assert np.all(acc == 0), acc[:3]
+    assert stats["cells"] >= 1
