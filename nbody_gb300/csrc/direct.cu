@@ -404,8 +404,10 @@ namespace nbg
         const size_t tb = std::max<size_t>(1, (n + per - 1) / per);
         const size_t slots = static_cast<size_t>(occupancy(v.fn[li][ai], v.block)) * sms;
         // Split the sources so tb*js CTAs pack into whole waves: minimise the padded
-        // work ceil(tb*js/slots)*slots/(tb*js) per unit, preferring fewer chunks.
-        const size_t max_js = std::max<size_t>(1, std::min<size_t>(64, n / (kTile * 4)));
+        // work ceil(tb*js/slots)*slots/(tb*js) per unit, preferring fewer chunks. Chunks may
+        // be a single tile: at small n the target blocks alone would leave most SMs idle
+        // (N = 4096 has 32 target blocks of 128).
+        const size_t max_js = std::max<size_t>(1, std::min<size_t>(64, n / kTile));
         size_t best_js = 1;
         double best_cost = 1e300;
         for (size_t js = 1; js <= max_js; ++js)
