@@ -81,7 +81,7 @@ namespace nbg
         void* temp = nullptr;           // sort and scan temporaries
         size_t temp_bytes = 0;
         BoxParams* box = nullptr;
-        double* bbox_part = nullptr;
+        float* bbox_part = nullptr;
         unsigned long long* stats = nullptr;   // [0] interactions, [1] node visits, [2] octree nodes,
                                                // [3] the traversal's tile counter
         const uint32_t* order = nullptr;       // sorted indices of the last build (keys/vals ping-pong)
@@ -100,7 +100,7 @@ namespace nbg
     // all axes), which fix the fixed-point scale of the cell sums. Min and max are exact,
     // so the float fold equals a double one; the partials are widened at the end.
     __global__ void __launch_bounds__(256) bbox_partial_kernel(const float4* __restrict__ src, const int stride,
-                                                               const int n, double* __restrict__ part)
+                                                               const int n, float* __restrict__ part)
     {
         float v[kBboxVals] = { INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.f, 0.f };
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -138,30 +138,31 @@ namespace nbg
             __syncthreads();
         }
         if (threadIdx.x < kBboxVals)
-            part[blockIdx.x * kBboxVals + threadIdx.x] = static_cast<double>(red[threadIdx.x][0]);
+            part[blockIdx.x * kBboxVals + threadIdx.x] = red[threadIdx.x][0];
     }
 
     // The exponent e with 0 <= v < 2^e for a finite float v >= 0 (v = M 2^(E - 150) with
     // M < 2^24, so v < 2^(E - 126); subnormals and zero lie below 2^-126).
-    __device__ __forceinline__ int bound_exp(const double v)
+    __device__ __forceinline__ int bound_exp(const float v)
     {
-        const uint32_t E = (__float_as_uint(static_cast<float>(v)) >> 23) & 0xffu;
+        const uint32_t E = (__float_as_uint(v) >> 23) & 0xffu;
         return (E ? static_cast<int>(E) : 1) - 126;
     }
 
-    __global__ void __launch_bounds__(256) box_final_kernel(const double* __restrict__ part, const int nparts,
+    __global__ void __launch_bounds__(256) box_final_kernel(const float* __restrict__ part, const int nparts,
                                                             const int n, const int mode, const float size,
                                                             BoxParams* __restrict__ box)
     {
-        // one block folds the per-block partials (a strided pass, then a tree)
-        __shared__ double red[kBboxVals][256];
-        double v[kBboxVals] = { INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.0, 0.0 };
+        // one block folds the per-block partials (a strided pass, then a tree), in float:
+        // min and max are exact
+        __shared__ float red[kBboxVals][256];
+        float v[kBboxVals] = { INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.f, 0.f };
         for (int k = threadIdx.x; k < nparts; k += blockDim.x)
         {
             for (int a = 0; a < 3; ++a)
-                v[a] = fmin(v[a], part[k * kBboxVals + a]);
+                v[a] = fminf(v[a], part[k * kBboxVals + a]);
             for (int a = 3; a < kBboxVals; ++a)
-                v[a] = fmax(v[a], part[k * kBboxVals + a]);
+                v[a] = fmaxf(v[a], part[k * kBboxVals + a]);
         }
         for (int a = 0; a < kBboxVals; ++a)
             red[a][threadIdx.x] = v[a];
@@ -171,9 +172,9 @@ namespace nbg
             if (threadIdx.x < s)
             {
                 for (int a = 0; a < 3; ++a)
-                    red[a][threadIdx.x] = fmin(red[a][threadIdx.x], red[a][threadIdx.x + s]);
+                    red[a][threadIdx.x] = fminf(red[a][threadIdx.x], red[a][threadIdx.x + s]);
                 for (int a = 3; a < kBboxVals; ++a)
-                    red[a][threadIdx.x] = fmax(red[a][threadIdx.x], red[a][threadIdx.x + s]);
+                    red[a][threadIdx.x] = fmaxf(red[a][threadIdx.x], red[a][threadIdx.x + s]);
             }
             __syncthreads();
         }
@@ -204,22 +205,27 @@ namespace nbg
             double ext = 0.0;
             for (int a = 0; a < 3; ++a)
                 ext = fmax(ext, hi[a] - lo[a]);
+            // the smallest power of two above ext (ext = f 2^k with f in [0.5, 1), so 2^k),
+            // which keeps the maximum strictly inside the top cell; 1 for a zero or
+            // non-finite extent
             double e = 1.0;
             if (ext > 0.0 && isfinite(ext))
-                e = exp2(ceil(log2(ext)));
-            if (e <= ext)
-                e *= 2.0;       // keep the maximum strictly inside the top cell
+            {
+                int k = 0;
+                frexp(ext, &k);
+                e = ldexp(1.0, k);
+            }
             // centre the cube on the bodies, then move its corner down onto the cell grid
             // (a shift of less than one cell); double the edge if that would uncover the
-            // maximum
+            // maximum. Cells are powers of two, so dividing by one is an exact multiply.
             for (int pass = 0; pass < 2; ++pass)
             {
-                const double cell = e / static_cast<double>(1u << kMortonBits);
+                const double cell = ldexp(e, -kMortonBits), per_cell = ldexp(1.0 / e, kMortonBits);
                 bool fits = true;
                 for (int a = 0; a < 3; ++a)
                 {
                     const double c = isfinite(lo[a]) ? 0.5 * (lo[a] + hi[a]) : 0.0;
-                    b.lo[a] = floor((c - 0.5 * e) / cell) * cell;
+                    b.lo[a] = floor((c - 0.5 * e) * per_cell) * cell;
                     b.center[a] = b.lo[a] + 0.5 * e;
                     fits = fits && (!isfinite(hi[a]) || hi[a] < b.lo[a] + e);
                 }
@@ -1134,7 +1140,7 @@ namespace nbg
             {
                 cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&b.box), sizeof(BoxParams), ctx->stream);
                 if (e == cudaSuccess)
-                    e = cudaMallocAsync(reinterpret_cast<void**>(&b.bbox_part), kBboxBlocks * kBboxVals * sizeof(double),
+                    e = cudaMallocAsync(reinterpret_cast<void**>(&b.bbox_part), kBboxBlocks * kBboxVals * sizeof(float),
                                         ctx->stream);
                 if (e == cudaSuccess)
                     e = cudaMallocAsync(reinterpret_cast<void**>(&b.stats), 4 * sizeof(unsigned long long), ctx->stream);

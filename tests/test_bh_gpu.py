@@ -89,11 +89,11 @@ def test_morton_and_sort_order_bit_exact(gpu):
             assert np.array_equal(codes, ref_codes[ref_order])
 
 
-@pytest.mark.parametrize("n", [2, 3, 4095, 4096, 4097, 12289, 1 << 20])
+@pytest.mark.parametrize("n", [2, 3, 1023, 1024, 1025, 4095, 4096, 4097, 12289, 1 << 20, (1 << 22) - 1, (1 << 22) + 1])
 def test_sort_order_at_tile_edges(gpu, n):
     """The radix sort (one kernel per digit pass, decoupled look-back between 4096-key
-    tiles) against the oracle's stable order, at sizes on and next to the tile size, with
-    runs of equal codes (ties keep index order)."""
+    tiles) against the oracle's stable order, at sizes on and next to multiples of a tile
+    and of a warp's share of one, with runs of equal codes (ties keep index order)."""
     rng = np.random.default_rng(n)
     b = np.zeros((n, 12), np.float32)
     b[:, :3] = rng.uniform(-30, 30, (n, 3)).astype(np.float32)
