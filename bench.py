@@ -697,11 +697,15 @@ def bench_small_configs(torch, stream, flush, native, scenes):
         ctx.set_stream(stream.cuda_stream)
         ctx.upload_bodies(b)
         ctx.update(p, 3)
+        ctx.update_graph(p, 3)
         torch.cuda.synchronize()
-        ms = timed_steps(torch, stream, flush, lambda: ctx.update(p, 200), 1)[0]
+        ms_eager = timed_steps(torch, stream, flush, lambda: ctx.update(p, 200), 1)[0]
+        ms_graph = timed_steps(torch, stream, flush, lambda: ctx.update_graph(p, 200), 1)[0]
         stats = ctx.bh_stats()
+    ms = min(ms_eager, ms_graph)
     cpu_s, cores = cpu_barnes_hut_rate(b, 64.0, 0.5)
-    out["config2_two_plummer_bh"] = {"n_bodies": len(b), "steps": 200, "ms": ms, "steps_per_s": 200 / (ms * 1e-3),
+    out["config2_two_plummer_bh"] = {"n_bodies": len(b), "steps": 200, "ms": ms, "ms_eager": ms_eager,
+                                     "ms_graph": ms_graph, "steps_per_s": 200 / (ms * 1e-3),
                                      "body_steps_per_s": len(b) * 200 / (ms * 1e-3),
                                      "interactions_per_body": stats["interactions"] / len(b),
                                      "cpu_reference_bh_step_s": cpu_s, "cpu_cores": cores,

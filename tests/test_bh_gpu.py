@@ -455,3 +455,21 @@ def test_bh_all_bodies_at_one_point(gpu, law, tree_box):
     acc, stats = bh_accel(gpu, b, theta=0.5, law=law, eps2=1e-4 if law == 1 else 0.0, size=64.0, tree_box=tree_box)
     assert np.all(acc == 0), acc[:3]
     assert stats["cells"] >= 1
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp32", "compensated"])
+def test_bh_graph_replay_equals_eager(gpu, precision):
+    """A Barnes-Hut step captured as a CUDA graph (nbody_cuda_update_graph) replays the whole
+    build and walk on the device with no host round trip, and gives the same bits as eager
+    steps."""
+    from nbody_gb300 import scenes
+    b = scenes.two_plummer(10000)
+    p = gpu.params(mode=gpu.MODE_NLOGN, theta=0.5, dt=5e-4, eps2=1e-4, law=gpu.LAW_SOFTENED, size=0.0, tree_box=1,
+                   precision=precision)
+    out = []
+    for graph in (False, True):
+        with gpu.Context() as ctx:
+            ctx.upload_bodies(b)
+            (ctx.update_graph if graph else ctx.update)(p, 12)
+            out.append(ctx.download_bodies())
+    assert np.array_equal(out[0], out[1])
