@@ -5,7 +5,7 @@ Tolerances (stated once, used throughout):
     within a few 1e-5 * scale_i of the exact sum -- the reference's own CPU solver is
     1.9e-5 * scale_i from FP64 on the 1024-body disk (tests/test_oracle.py).
   * FP32 direct sum vs the reference (and vs FP64): max |da_i| / scale_i <= 5e-5 and
-    median <= 1e-5 (the BASELINE tolerance for direct sum).
+    median <= 1e-5 (the stated direct-sum tolerance: <= 1e-5 relative).
   * integrate: bit-identical to the reference's CPU integrator.
 """
 import numpy as np

@@ -1,6 +1,6 @@
 """Split-precision (compensated) and FP64 forms on the GPU, against the FP64 oracle.
 
-Bars (BASELINE: compensated median relative acceleration error <= 1e-6 against FP64):
+Bars (the target: compensated median relative acceleration error <= 1e-6 against FP64):
   * compensated direct sum: median |a - a64| / |a64| <= 1e-6; per body
     |a - a64| <= 2e-6 * sum_j |a_ij| (the float rounding of the result alone is ~6e-8 |a|);
   * FP64 direct sum: |a - a64| <= 1e-12 * sum_j |a_ij| (different summation order only);
