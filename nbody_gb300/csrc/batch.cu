@@ -566,9 +566,9 @@ namespace nbg
         q.law = NBODY_LAW_SOFTENED;
         if (!(q.eps2 > 0.f))
             q.eps2 = 1e-4f;
-        cudaEvent_t e0, e1;
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
+        EventPair ev;
+        if (ev.status != cudaSuccess)
+            return ctx_cuda_fail(ctx, ev.status, "event create");
         int best_i = 0;
         float best_ms = 1e30f;
         for (int i = 0; i < batch_config_count(); ++i)
@@ -578,17 +578,11 @@ namespace nbg
             float ms_best = 1e30f;
             for (int rep = 0; rep < 3; ++rep)
             {
-                cudaEventRecord(e0, ctx->stream);
+                cudaEventRecord(ev.start, ctx->stream);
                 if (const int st = batch_accelerate(ctx, &q))
-                {
-                    cudaEventDestroy(e0);
-                    cudaEventDestroy(e1);
                     return st;
-                }
-                cudaEventRecord(e1, ctx->stream);
-                cudaEventSynchronize(e1);
-                float ms = 0;
-                cudaEventElapsedTime(&ms, e0, e1);
+                cudaEventRecord(ev.stop, ctx->stream);
+                const float ms = ev.elapsed_ms();
                 if (rep > 0)
                     ms_best = std::min(ms_best, ms);
             }
@@ -600,8 +594,6 @@ namespace nbg
                 best_i = i;
             }
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
         b.config = best_i;
         b.items_config = -1;
         b.tuned = true;

@@ -50,25 +50,23 @@ extern "C" int nbody_cuda_calibrate_fp32(nbody_cuda* ctx, double* tflops_scalar,
     if (const int st = ensure_scratch(ctx, static_cast<size_t>(blocks) * threads * sizeof(float)))
         return st;
     float* out = static_cast<float*>(ctx->scratch);
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    EventPair ev;
+    if (ev.status != cudaSuccess)
+        return ctx_cuda_fail(ctx, ev.status, "event create");
     double res[2] = { 0, 0 };
     for (int packed = 0; packed < 2; ++packed)
     {
         float best = 1e30f;
         for (int rep = 0; rep < 4; ++rep)
         {
-            cudaEventRecord(e0, ctx->stream);
+            cudaEventRecord(ev.start, ctx->stream);
             if (packed)
                 ffma_peak_kernel<true><<<blocks, threads, 0, ctx->stream>>>(out, iters, 0.999f, 1e-3f);
             else
                 ffma_peak_kernel<false><<<blocks, threads, 0, ctx->stream>>>(out, iters, 0.999f, 1e-3f);
             ++ctx->launches;
-            cudaEventRecord(e1, ctx->stream);
-            cudaEventSynchronize(e1);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
+            cudaEventRecord(ev.stop, ctx->stream);
+            const float ms = ev.elapsed_ms();
             if (rep > 0 && ms < best)
                 best = ms;
         }
@@ -76,8 +74,6 @@ extern "C" int nbody_cuda_calibrate_fp32(nbody_cuda* ctx, double* tflops_scalar,
         const double flop = static_cast<double>(blocks) * threads * iters * 8.0 * 2.0 * 2.0;
         res[packed] = flop / (best * 1e-3) / 1e12;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return ctx_cuda_fail(ctx, e, "calibration kernel");
@@ -120,24 +116,20 @@ extern "C" int nbody_cuda_calibrate_fp64(nbody_cuda* ctx, double* tflops)
     const int blocks = sms * 4, threads = 256, iters = 1 << 10;
     if (const int st = ensure_scratch(ctx, static_cast<size_t>(blocks) * threads * sizeof(double)))
         return st;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    EventPair ev;
+    if (ev.status != cudaSuccess)
+        return ctx_cuda_fail(ctx, ev.status, "event create");
     float best = 1e30f;
     for (int rep = 0; rep < 4; ++rep)
     {
-        cudaEventRecord(e0, ctx->stream);
+        cudaEventRecord(ev.start, ctx->stream);
         dfma_peak_kernel<<<blocks, threads, 0, ctx->stream>>>(static_cast<double*>(ctx->scratch), iters, 0.999, 1e-3);
         ++ctx->launches;
-        cudaEventRecord(e1, ctx->stream);
-        cudaEventSynchronize(e1);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventRecord(ev.stop, ctx->stream);
+        const float ms = ev.elapsed_ms();
         if (rep > 0 && ms < best)
             best = ms;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return ctx_cuda_fail(ctx, e, "calibration kernel");

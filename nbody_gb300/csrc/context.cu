@@ -700,17 +700,13 @@ int nbody_cuda_direct_autotune(nbody_cuda* ctx, const nbody_step_params* p, doub
     nbody_step_params q = *p;
     q.mode = NBODY_MODE_N2;
     q.precision = NBODY_PREC_FP32;
-    cudaEvent_t e0, e1;
-    NBG_CUDA(ctx, cudaEventCreate(&e0), "event create");
-    NBG_CUDA(ctx, cudaEventCreate(&e1), "event create");
+    EventPair ev;
+    if (ev.status != cudaSuccess)
+        return cuda_fail(ctx, ev.status, "event create");
     // one untimed launch first, so the clocks are up before the first shape is timed
     ctx->force_variant = -1;
     if (const int st = direct_accel(ctx, &q, false))
-    {
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
         return st;
-    }
     int best_i = 0;
     float best_ms = 1e30f;
     for (int i = 0; i < direct_variant_count(); ++i)
@@ -719,20 +715,15 @@ int nbody_cuda_direct_autotune(nbody_cuda* ctx, const nbody_step_params* p, doub
         float ms_best = 1e30f;
         for (int rep = 0; rep < 2; ++rep)
         {
-            cudaEventRecord(e0, ctx->stream);
+            cudaEventRecord(ev.start, ctx->stream);
             const int st = direct_accel(ctx, &q, false);
-            cudaEventRecord(e1, ctx->stream);
+            cudaEventRecord(ev.stop, ctx->stream);
             if (st != NBODY_OK)
             {
-                cudaEventDestroy(e0);
-                cudaEventDestroy(e1);
                 ctx->force_variant = -1;
                 return st;
             }
-            cudaEventSynchronize(e1);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            ms_best = std::min(ms_best, ms);
+            ms_best = std::min(ms_best, ev.elapsed_ms());
         }
         if (times_ms && static_cast<size_t>(i) < ntimes)
             times_ms[i] = ms_best;
@@ -742,8 +733,6 @@ int nbody_cuda_direct_autotune(nbody_cuda* ctx, const nbody_step_params* p, doub
             best_i = i;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     ctx->force_variant = best_i;
     if (best)
         *best = best_i;

@@ -110,6 +110,37 @@ namespace nbg
 {
     int ctx_fail(nbody_cuda* ctx, int status, const char* msg);
     int ctx_cuda_fail(nbody_cuda* ctx, cudaError_t e, const char* what);
+
+    // Two timing events for host-side measurement loops, destroyed with the object.
+    // `status` is the first creation error, if any.
+    struct EventPair
+    {
+        cudaEvent_t start = nullptr, stop = nullptr;
+        cudaError_t status = cudaSuccess;
+        EventPair()
+        {
+            status = cudaEventCreate(&start);
+            if (status == cudaSuccess)
+                status = cudaEventCreate(&stop);
+        }
+        ~EventPair()
+        {
+            if (start)
+                cudaEventDestroy(start);
+            if (stop)
+                cudaEventDestroy(stop);
+        }
+        EventPair(const EventPair&) = delete;
+        EventPair& operator=(const EventPair&) = delete;
+        // milliseconds between the two recorded events, after waiting for the second
+        float elapsed_ms() const
+        {
+            float ms = 0.f;
+            if (cudaEventSynchronize(stop) == cudaSuccess)
+                cudaEventElapsedTime(&ms, start, stop);
+            return ms;
+        }
+    };
     int ensure_scratch(nbody_cuda* ctx, size_t bytes);
     // Every growth of a device buffer goes through here: refused during graph capture (the
     // pointers a graph holds must stay valid), and it retires any captured graph.
