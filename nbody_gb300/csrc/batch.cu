@@ -544,9 +544,11 @@ namespace nbg
             return NBODY_OK;
         const BatchFn fn = p->law == NBODY_LAW_SOFTENED ? c.soft : c.cutoff;
         const int grid = occupancy_grid(ctx, fn, c.block, b.nitems);
-        cudaMemsetAsync(b.counter, 0, sizeof(unsigned), ctx->stream);
-        if (b.nblocks)
-            cudaMemsetAsync(b.block_done, 0, static_cast<size_t>(b.nblocks) * sizeof(unsigned), ctx->stream);
+        cudaError_t me = cudaMemsetAsync(b.counter, 0, sizeof(unsigned), ctx->stream);
+        if (me == cudaSuccess && b.nblocks)
+            me = cudaMemsetAsync(b.block_done, 0, static_cast<size_t>(b.nblocks) * sizeof(unsigned), ctx->stream);
+        if (me != cudaSuccess)
+            return ctx_cuda_fail(ctx, me, "batched counters");
         fn<<<grid, c.block, 0, ctx->stream>>>(ctx->pm, ctx->vr, b.d_items, b.nitems, c.chunk, b.counter, ctx->acc,
                                               b.partial, b.block_done, p->G, p->eps2, ctx->dev_error);
         ++ctx->launches;

@@ -1214,7 +1214,8 @@ namespace nbg
         const unsigned blocks = ceil_div(n, 256);
         uint64_t& L = ctx->launches;
 
-        cudaMemsetAsync(b.stats, 0, 4 * sizeof(unsigned long long), s);
+        if (const cudaError_t me = cudaMemsetAsync(b.stats, 0, 4 * sizeof(unsigned long long), s))
+            return ctx_cuda_fail(ctx, me, "tree statistics");
         // tree_box = 0 is the reference's fixed root box; it needs a positive size
         const bool auto_box = p->tree_box != 0 || !(p->size > 0.f);
         // the bounds pass runs for the fixed box too: the cell sums' scale comes from it
@@ -1297,12 +1298,13 @@ namespace nbg
         if (n < 2)
         {
             // a lone body feels nothing (its own leaf is cut off / multiplied by d = 0)
+            cudaError_t me = cudaSuccess;
             if (acc)
-                cudaMemsetAsync(acc, 0, n * sizeof(float4), s);
+                me = cudaMemsetAsync(acc, 0, n * sizeof(float4), s);
             else
-                for (size_t i = 0; i < n; ++i)
-                    cudaMemsetAsync(body_out + i * 12 + 8, 0, 3 * sizeof(float), s);
-            return NBODY_OK;
+                for (size_t i = 0; i < n && me == cudaSuccess; ++i)
+                    me = cudaMemsetAsync(body_out + i * 12 + 8, 0, 3 * sizeof(float), s);
+            return me == cudaSuccess ? NBODY_OK : ctx_cuda_fail(ctx, me, "lone-body acceleration");
         }
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
