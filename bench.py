@@ -30,7 +30,9 @@ Printed JSON line (rank 0):
                   bandwidth, and one frame of update + state(). Its "cpu_reference_bh"
                   object times one full step of the restated CPU Barnes-Hut on the same
                   bodies on all host cores.
-  configs         configs 1 (N = 4096 Plummer, 100 steps) and 2 (2 x 131072 Plummer BH).
+  configs         configs 1 (N = 4096 Plummer, 100 steps) and 2 (2 x 131072 Plummer BH),
+                  each beside the reference's CPU solver on the same bodies and host cores
+                  (all 100 steps of config 1; one step of config 2).
   scene_generators util::disk and util::cube on the device at N = 16,777,216, against the
                   reference's serial generator on 1,048,576 bodies.
   ray_query       Tree::query over the exported tree of 1,048,576 bodies: picking rays
@@ -166,6 +168,23 @@ def cpu_brute_force_rate(bodies: np.ndarray, seconds: float = 10.0):
         k = int(k * min(8.0, max(2.0, seconds / max(dt, 1e-3))))
     return k * n / dt, threads, "port", \
         f"{k} sampled targets x all {n} sources (restated reference brute force), {dt:.1f} s"
+
+
+def cpu_config1_seconds(bodies, steps, dt):
+    """Seconds for `steps` whole updates (accelerate + integrate) of the reference CPU brute
+    force on all host cores: Sim::update (sim.cpp:307-313, Solver::update solver.h:59) over
+    CpuBruteForceSolver -- the reference's own build where present, else its restatement."""
+    from oracle import oracle as O
+    threads = O.threads()
+    if O.ref_available():
+        t0 = time.perf_counter()
+        O.ref_brute_force(bodies, 1.0, steps=steps, dt=dt, nthreads=threads)
+        return time.perf_counter() - t0, threads, "reference (CpuBruteForceSolver, reference law)"
+    b = bodies
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        b = O.integrate(O.brute_force(b, 1.0, nthreads=threads), dt, 10000.0, False)
+    return time.perf_counter() - t0, threads, "port (restated CpuBruteForceSolver + integrate)"
 
 
 def cpu_barnes_hut_rate(bodies, size, theta):
@@ -687,8 +706,11 @@ def bench_small_configs(torch, stream, flush, native, scenes):
         torch.cuda.synchronize()
         ms = timed_steps(torch, stream, flush, lambda: ctx.update(p, 100), 1)[0]
         ms_graph = timed_steps(torch, stream, flush, lambda: ctx.update_graph(p, 100), 1)[0]
+    cpu_s, cores, kind = cpu_config1_seconds(b, 100, 1e-3)
     out["config1_plummer_4096"] = {"steps": 100, "ms_eager": ms, "ms_graph": ms_graph,
-                                   "body_steps_per_s": 4096 * 100 / (min(ms, ms_graph) * 1e-3)}
+                                   "body_steps_per_s": 4096 * 100 / (min(ms, ms_graph) * 1e-3),
+                                   "cpu_100_steps_s": cpu_s, "cpu_body_steps_per_s": 4096 * 100 / cpu_s,
+                                   "cpu_cores": cores, "cpu_kind": kind}
     # config 2: two Plummer spheres, BH theta 0.5 (reference convention), 200 steps
     b = scenes.two_plummer(131072)
     p = native.params(mode=native.MODE_NLOGN, theta=0.5, dt=5e-4, eps2=1e-4, law=native.LAW_SOFTENED,
