@@ -64,3 +64,29 @@ def test_bh_mass_scaling_at_16m(gpu):
     a2 = accel(gpu, b, p)
     assert np.all(np.isfinite(a1))
     assert np.array_equal(a2, 2.0 * a1)
+
+
+def test_batched_mass_scaling_and_momentum(gpu):
+    """The batched form on the 512 Plummer systems of log-uniform size in [64, 8192]
+    (773,681 bodies): a(2m) == 2 a(m) bit for bit, and every system's own momentum
+    residual stays within TOL_MOMENTUM (systems never interact)."""
+    from nbody_gb300 import scenes
+    b, off = scenes.batch_plummer()
+    p = gpu.params(mode=gpu.MODE_BATCHED, law=gpu.LAW_SOFTENED, eps2=1e-4)
+    out = []
+    for scale in (1.0, 2.0):
+        bb = b.copy()
+        bb[:, 7] *= scale
+        with gpu.Context() as ctx:
+            ctx.upload_bodies(bb)
+            ctx.set_systems(off)
+            ctx.accelerate(p)
+            out.append(ctx.download_bodies()[:, 8:11].copy())
+    a1, a2 = out
+    assert np.all(np.isfinite(a1))
+    assert np.array_equal(a2, 2.0 * a1)
+    m = b[:, 7].astype(np.float64)
+    a = a1.astype(np.float64)
+    mom = np.add.reduceat(m[:, None] * a, off[:-1], axis=0)
+    mag = np.add.reduceat(m * np.linalg.norm(a, axis=1), off[:-1])
+    assert np.all(np.linalg.norm(mom, axis=1) <= TOL_MOMENTUM * mag)
