@@ -34,3 +34,19 @@ def test_reference_arm_runs():
     # a CPU direct sum of 2^20 bodies takes minutes per step on any host: well under 1e5 body-steps/s
     assert 0 < line["value"] < 1e5
     assert line["ms_per_step"] > 1e3
+
+
+@pytest.mark.parametrize("use_ref", [True, False], ids=["reference", "port"])
+def test_config1_cpu_timing_runs_both_paths(monkeypatch, use_ref):
+    """The config-1 CPU leg: all steps of the reference brute force where its build loads,
+    else the restated solver and integrator, timed on the same bodies."""
+    from nbody_gb300 import scenes
+    from oracle import oracle as O
+    if use_ref and not O.ref_available():
+        pytest.skip("the reference's own CPU build is not present here")
+    if not use_ref:
+        monkeypatch.setattr(O, "ref_available", lambda: False)
+    b = scenes.plummer(256, seed=1001)
+    s, cores, kind = bench.cpu_config1_seconds(b, 3, 1e-3)
+    assert s > 0 and cores >= 1
+    assert kind.startswith("reference" if use_ref else "port")
