@@ -228,3 +228,36 @@ def test_morton_cells_match_reference_octants():
 def test_sort_order_stable():
     codes = np.array([5, 3, 5, 1, 3, 3], np.uint64)
     assert list(O.sort_order(codes)) == [3, 1, 4, 5, 0, 2]
+
+
+# --- properties of the reference semantics (the ones the GPU tests check at full size) ----
+
+def test_reference_semantics_scale_exactly_with_mass():
+    """Doubling every mass doubles every acceleration bit for bit in the reference's brute
+    force and in its octree (the running-mean centres of mass of bhtree.cpp:87-95 are
+    unchanged by a power-of-two factor), both in the restatement and, where it was built,
+    in the reference itself."""
+    from nbody_gb300 import scenes
+    b = scenes.plummer(2048, seed=11)
+    b2 = b.copy()
+    b2[:, 7] *= 2.0
+    bf = [O.brute_force(x, 1.0)[:, 8:11] for x in (b, b2)]
+    assert np.array_equal(bf[1], 2.0 * bf[0])
+    bh = [O.barnes_hut(x, 64.0, 0.5, 1.0)[0][:, 8:11] for x in (b, b2)]
+    assert np.array_equal(bh[1], 2.0 * bh[0])
+    if O.ref_available():
+        rb = [O.ref_barnes_hut(x, 64.0, 0.5, 1.0)[:, 8:11] for x in (b, b2)]
+        assert np.array_equal(rb[1], 2.0 * rb[0])
+        assert np.array_equal(rb[0], bh[0])
+
+
+def test_reference_brute_force_momentum_residual():
+    """With every radius 0 the reference's force law is antisymmetric, so sum_i m_i a_i = 0
+    up to FP32 rounding. Its own sequential FP32 sum leaves under 1e-7 of sum_i m_i |a_i|
+    (about 3e-8 measured): the GPU property tests bound the same residual by 1e-6."""
+    from nbody_gb300 import scenes
+    b = scenes.plummer(4096, seed=12)
+    a = O.brute_force(b, 1.0)[:, 8:11].astype(np.float64)
+    m = b[:, 7].astype(np.float64)
+    res = np.linalg.norm((m[:, None] * a).sum(0)) / (m * np.linalg.norm(a, axis=1)).sum()
+    assert res < 1e-7
