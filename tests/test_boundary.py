@@ -1,7 +1,6 @@
 """The C-ABI boundary without compute: the library builds, loads, exports every symbol
 include/*.h declares, and reports failures the reference's way (a probe that returns a
 reason, source/gpu.cpp:115-149; a constructor failure turned into a status)."""
-import os
 import re
 
 from conftest import ROOT

@@ -17,7 +17,6 @@ Bars:
 import numpy as np
 import pytest
 
-from conftest import golden
 from oracle import oracle as O
 from test_scenes import CASES, case_names, kwargs_from
 
