@@ -345,9 +345,9 @@ def _bench_gpu(args, stream):
                          "traffic": MEASURED_TRAFFIC.get((cfg["targets_per_thread"], cfg["block"],
                                                           native.Context.direct_variant(tuned)["packed"],
                                                           cfg["jsplit"])),
-                         "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one N=2^20 launch of the "
-                                         "chosen shape (profiles/direct_fp32_n262144_full.md); null for a shape "
-                                         "not captured"},
+                         "traffic_source": "constant: ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                           "N=2^20 launch of the chosen shape, captured earlier with the "
+                                           "profiler, not measured in this run; null for a shape not captured"},
             "cpu_baseline": {"value": cpu_rate / N, "unit": "body-steps/s", "cores": cores, "kind": kind,
                              "sample": sample + "; body-steps/s = pairs/s / N", "pairs_per_s": cpu_rate},
             "clocks": clocks.summary(),

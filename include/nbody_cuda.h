@@ -252,7 +252,8 @@ int nbody_cuda_synchronize(nbody_cuda* ctx);
  *     beyond the context's scratch) ------------------------------------------------------ */
 
 /* Direct-sum accelerations over split streams already resident on the device:
- * pos_mass, vel_radius (radius read for the CUTOFF law only), acc out; n bodies.
+ * pos_mass, vel_radius (radius read for the CUTOFF law only), acc out; n bodies. Each
+ * stream the kernel reads must be 16-byte aligned (NBODY_ERR_INVALID otherwise).
  * The device twin of accelerate_split.comp N2 mode (shaders/accelerate_split.comp:9-18). */
 int nbody_cuda_dev_accel_soa(nbody_cuda* ctx, const void* pos_mass, const void* vel_radius,
                              void* acc, size_t n, const nbody_step_params* p);
@@ -275,10 +276,15 @@ int nbody_cuda_dev_integrate_soa(nbody_cuda* ctx, void* pos_mass, void* vel_radi
  * library, which every GPU that loads the library holds until the process exits. Hence
  * n <= 1048576; a larger n returns NBODY_ERR_INVALID. Work is queued on `stream` (a
  * cudaStream_t; NULL is the default stream) and waited for before the call returns;
- * NBODY_ERR_TIMEOUT reports a device-side wait that gave up. The first call on each
- * device looks up the array's device address (cudaGetSymbolAddress); make that first
- * call before any stream capture. All calls share the one array, so calls that overlap
- * on the GPU (from other host threads or streams) race: the caller must serialise them. */
+ * NBODY_ERR_TIMEOUT reports a device-side wait that gave up. The call is synchronous:
+ * it returns after the kernel has finished. The first call in each CUDA context (the
+ * device's primary context, also after cudaDeviceReset re-creates it, or any context
+ * the caller made current) looks up the array's device address (cudaGetSymbolAddress)
+ * and caches it under that context's id; make that first call before any stream
+ * capture. All calls share the one array and its error word, so calls that overlap on
+ * the GPU (from other host threads or streams) race: the caller must serialise them.
+ * Every pointer the kernel reads as float4 must be 16-byte aligned: pos_mass, acc, and
+ * vel_radius under the CUTOFF law; otherwise NBODY_ERR_INVALID before any launch. */
 int nbody_cuda_dev_accel_soa_noalloc(const void* pos_mass, const void* vel_radius, void* acc,
                                      size_t n, const nbody_step_params* p, void* stream);
 

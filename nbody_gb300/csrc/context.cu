@@ -899,7 +899,8 @@ int nbody_cuda_dev_accel_soa(nbody_cuda* ctx, const void* pos_mass, const void* 
         return NBODY_OK;
     if (!pos_mass || !acc || (p->law == NBODY_LAW_CUTOFF && !vel_radius))
         return fail(ctx, NBODY_ERR_INVALID, "null device buffer");
-    if ((reinterpret_cast<uintptr_t>(pos_mass) | reinterpret_cast<uintptr_t>(acc)) & 15u)
+    const uintptr_t vr = p->law == NBODY_LAW_CUTOFF ? reinterpret_cast<uintptr_t>(vel_radius) : 0;
+    if ((reinterpret_cast<uintptr_t>(pos_mass) | reinterpret_cast<uintptr_t>(acc) | vr) & 15u)
         return fail(ctx, NBODY_ERR_INVALID, "device buffers must be 16-byte aligned");
     if (n > static_cast<size_t>(INT32_MAX / 4))
         return fail(ctx, NBODY_ERR_INVALID, "body count too large");

@@ -11,10 +11,15 @@
 // is part of the loaded module: every GPU that loads the library holds it (16 MiB of
 // partial sums plus one error word) until the process exits. Host code cannot pass the
 // array's name to a kernel -- on the host that name is only a stand-in for the symbol,
-// not a device address -- so the address is looked up with cudaGetSymbolAddress once per
-// device, with that device current, and cached.
+// not a device address -- so the address is looked up with cudaGetSymbolAddress, with
+// the device current, once per CUDA context, and cached under that context's unique id.
+// The module is loaded anew in every context (a second context on the same device, or
+// the primary context re-created after cudaDeviceReset), so an address is never reused
+// outside the context it came from.
 #include <algorithm>
 #include <mutex>
+
+#include <cuda.h>       // CUcontext and CUresult only: the two driver calls are resolved at run time
 
 #include "common.cuh"
 #include "direct.cuh"
@@ -23,39 +28,92 @@ namespace
 {
     // Partial accelerations of the source chunks: jsplit * n float4 must fit.
     constexpr size_t kNoAllocPartials = size_t(1) << 20;   // 16 MiB of float4
-    constexpr int kMaxDevices = 64;
+    constexpr int kCacheSlots = 64;
 
     static __device__ __align__(256) float4 g_noalloc_partials[kNoAllocPartials];
     static __device__ __align__(256) unsigned g_noalloc_error;
 
     struct DeviceScratch
     {
+        unsigned long long ctx_id = 0;      // 0: an empty slot (context ids start at 1)
         float4* partials = nullptr;
         unsigned* error = nullptr;
     };
 
-    std::mutex g_setup_mutex;
-    DeviceScratch g_scratch[kMaxDevices];
+    using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+    using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
 
-    // Resolve the device addresses of the two arrays on the current device (first call on
-    // each device only). Returns a cudaError_t.
-    cudaError_t device_scratch(const int dev, DeviceScratch* out)
+    std::mutex g_setup_mutex;
+    DeviceScratch g_cache[kCacheSlots];
+    int g_next_slot = 0;
+    bool g_driver_resolved = false;
+    CtxGetCurrentFn g_get_current = nullptr;
+    CtxGetIdFn g_get_id = nullptr;
+
+    cudaError_t lookup(DeviceScratch* out)
+    {
+        void* p = nullptr;
+        void* e = nullptr;
+        cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (err != cudaSuccess)
+            return err;
+        err = cudaGetSymbolAddress(&e, g_noalloc_error);
+        if (err != cudaSuccess)
+            return err;
+        out->partials = static_cast<float4*>(p);
+        out->error = static_cast<unsigned*>(e);
+        return cudaSuccess;
+    }
+
+    // The device addresses of the two arrays in the calling thread's current context
+    // (the device's primary context unless the caller made another one current). The
+    // lookup runs on the first call in each context; later calls in the same context take
+    // the cached addresses. Where the driver cannot name the context, every call looks
+    // the addresses up again. Returns a cudaError_t.
+    cudaError_t device_scratch(DeviceScratch* out)
     {
         std::lock_guard<std::mutex> lock(g_setup_mutex);
-        DeviceScratch& s = g_scratch[dev];
-        if (!s.partials)
+        if (!g_driver_resolved)
         {
-            void* p = nullptr;
-            void* e = nullptr;
-            cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_partials);
-            if (err != cudaSuccess)
-                return err;
-            err = cudaGetSymbolAddress(&e, g_noalloc_error);
-            if (err != cudaSuccess)
-                return err;
-            s.partials = static_cast<float4*>(p);
-            s.error = static_cast<unsigned*>(e);
+            g_driver_resolved = true;
+            void* f = nullptr;
+            void* g = nullptr;
+            cudaDriverEntryPointQueryResult q1{}, q2{};
+            if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+                cudaGetDriverEntryPointByVersion("cuCtxGetId", &g, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+                q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess && f && g)
+            {
+                g_get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+                g_get_id = reinterpret_cast<CtxGetIdFn>(g);
+            }
+            cudaGetLastError();
         }
+        if (!g_get_current || !g_get_id)
+            return lookup(out);
+        CUcontext c = nullptr;
+        if (g_get_current(&c) != CUDA_SUCCESS || !c)
+        {
+            // no context current yet: the runtime call creates the primary context
+            if (const cudaError_t err = lookup(out))
+                return err;
+            if (g_get_current(&c) != CUDA_SUCCESS || !c)
+                return cudaSuccess;     // addresses looked up, but nothing to key them on
+        }
+        unsigned long long id = 0;
+        if (g_get_id(c, &id) != CUDA_SUCCESS || id == 0)
+            return lookup(out);
+        for (const DeviceScratch& s : g_cache)
+            if (s.ctx_id == id)
+            {
+                *out = s;
+                return cudaSuccess;
+            }
+        DeviceScratch s;
+        if (const cudaError_t err = lookup(&s))
+            return err;
+        s.ctx_id = id;
+        g_cache[g_next_slot] = s;
+        g_next_slot = (g_next_slot + 1) % kCacheSlots;
         *out = s;
         return cudaSuccess;
     }
@@ -79,14 +137,17 @@ extern "C" int nbody_cuda_dev_accel_soa_noalloc(const void* pos_mass, const void
         return NBODY_OK;
     if (!pos_mass || !acc || (p->law == NBODY_LAW_CUTOFF && !vel_radius))
         return NBODY_ERR_INVALID;
-    if ((reinterpret_cast<uintptr_t>(pos_mass) | reinterpret_cast<uintptr_t>(acc)) & 15u)
+    // every stream the kernel reads as float4 must be 16-byte aligned: the radii only under
+    // the CUTOFF law
+    const uintptr_t vr = p->law == NBODY_LAW_CUTOFF ? reinterpret_cast<uintptr_t>(vel_radius) : 0;
+    if ((reinterpret_cast<uintptr_t>(pos_mass) | reinterpret_cast<uintptr_t>(acc) | vr) & 15u)
         return NBODY_ERR_INVALID;
 
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    if (cudaGetDevice(&dev) != cudaSuccess)
         return NBODY_ERR_NO_DEVICE;
     DeviceScratch s;
-    if (device_scratch(dev, &s) != cudaSuccess)
+    if (device_scratch(&s) != cudaSuccess)
         return NBODY_ERR_CUDA;
 
     // The usual launch shape, with the source split capped so its partials fit.

@@ -1,8 +1,8 @@
 """Run one workload a fixed number of times and exit -- the target for profiler captures.
 
-    python -m nbody_gb300.run_case direct --n 262144 --steps 1
-    python -m nbody_gb300.run_case direct-aos --n 262144
-    python -m nbody_gb300.run_case integrate --n 16777216
+    python tests/run_case.py direct --n 262144 --steps 1
+    python tests/run_case.py direct-aos --n 262144
+    python tests/run_case.py integrate --n 16777216
 
 Inputs are the seeded scenes of :mod:`nbody_gb300.scenes`; nothing is timed or checked.
 """

@@ -54,6 +54,22 @@ def test_bad_layout_rejected(cuda_lib):
         raise AssertionError("an unknown layout must be rejected")
 
 
+def test_noalloc_rejects_misaligned_streams_before_any_cuda_call(cuda_lib):
+    """The allocation-free accelerate checks its arguments before it touches CUDA: a stream
+    it would read as float4 from an address that is not 16-byte aligned is NBODY_ERR_INVALID
+    (the radii only under the CUTOFF law, where the kernel reads them). No device is needed."""
+    import ctypes as C
+    from nbody_gb300 import native
+    f = cuda_lib.nbody_cuda_dev_accel_soa_noalloc
+    cut = native.params(law=native.LAW_CUTOFF)
+    soft = native.params(law=native.LAW_SOFTENED, eps2=1e-4)
+    ok, off = C.c_void_p(1 << 20), C.c_void_p((1 << 20) + 4)
+    assert f(ok, off, ok, 100, C.byref(cut), None) == native.ERR_INVALID
+    assert f(off, ok, ok, 100, C.byref(soft), None) == native.ERR_INVALID
+    assert f(ok, ok, off, 100, C.byref(soft), None) == native.ERR_INVALID
+    assert f(ok, None, ok, 100, C.byref(cut), None) == native.ERR_INVALID
+
+
 def test_step_params_layout():
     import ctypes
     from nbody_gb300 import native

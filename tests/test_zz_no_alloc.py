@@ -60,6 +60,42 @@ def test_noalloc_matches_context_entry_point(gpu, n, law, eps2):
         assert err.max() <= TOL_MAX and np.median(err) <= TOL_MEDIAN, (call, err.max())
 
 
+def test_noalloc_runs_while_allocation_is_refused(gpu, monkeypatch):
+    """The entry point's one promise: it allocates nothing. With every library allocation
+    made to fail (NBODY_CUDA_FAULT=alloc, the host-side injector), a context cannot grow its
+    scratch, yet two allocation-free calls in a row still succeed and agree bit for bit.
+    Device free memory is unchanged across the two calls."""
+    torch = pytest.importorskip("torch")
+    from nbody_gb300 import native, scenes
+
+    n = 200003
+    b = scenes.uniform_cube(n, seed=99)
+    pm = torch.from_numpy(np.ascontiguousarray(b[:, [0, 1, 2, 7]])).cuda()
+    vr = torch.from_numpy(np.ascontiguousarray(b[:, [4, 5, 6, 3]])).cuda()
+    p = native.params(law=1, eps2=1e-6)
+    stream = torch.cuda.current_stream().cuda_stream
+    L = native.lib()
+    outs = [torch.full_like(pm, float("nan")) for _ in range(2)]
+    torch.cuda.synchronize()
+    with native.Context() as ctx:        # the context path refuses to grow its scratch
+        ctx.set_stream(stream)
+        monkeypatch.setenv("NBODY_CUDA_FAULT", "alloc")
+        with pytest.raises(native.NbodyError) as e:
+            ctx.dev_accel_soa(pm.data_ptr(), vr.data_ptr(), outs[0].data_ptr(), n, p)
+        assert e.value.status == native.ERR_ALLOC
+    free = []
+    for acc in outs:
+        free.append(torch.cuda.mem_get_info()[0])
+        st = L.nbody_cuda_dev_accel_soa_noalloc(C.c_void_p(pm.data_ptr()), C.c_void_p(vr.data_ptr()),
+                                                C.c_void_p(acc.data_ptr()), n, C.byref(p), C.c_void_p(stream))
+        assert st == native.OK, st
+    free.append(torch.cuda.mem_get_info()[0])
+    a0, a1 = outs[0].cpu().numpy(), outs[1].cpu().numpy()
+    assert np.isfinite(a0[:, :3]).all()
+    assert np.array_equal(a0.view(np.uint32), a1.view(np.uint32))
+    assert free[1] == free[2], free
+
+
 def test_noalloc_rejects_oversize_and_bad_arguments(gpu):
     from nbody_gb300 import native
     L = native.lib()
