@@ -104,6 +104,34 @@ void orc_gravity(const float pos[3], const float radius, const float src[3],
     out[2] = (s * dz) / den;
 }
 
+/* The softened law the benchmark configurations use, G*m*d/(|d|^2 + eps2)^(3/2), written
+ * in the operation order of the reference's law above (physics.h:21-42) with eps2 added to
+ * |d|^2 and no cutoff. No reference counterpart: the reference has only the cutoff law. */
+void orc_gravity_softened(const float pos[3], const float src[3], const float src_mass, const float G,
+                          const float eps2, float out[3])
+{
+    const float dx = src[0] - pos[0];
+    const float dy = src[1] - pos[1];
+    const float dz = src[2] - pos[2];
+    const float dsq = ((dx * dx + dy * dy) + dz * dz) + eps2;
+    const float s = G * src_mass;
+    const float den = sqrtf(dsq) * dsq;
+    out[0] = (s * dx) / den;
+    out[1] = (s * dy) / den;
+    out[2] = (s * dz) / den;
+}
+
+/* One pair under either law (the visitor of cpu_brute_force.h:31-39 and
+ * cpu_barnes_hut.h:31-41, with the law chosen). */
+static inline void orc_pair(const int law, const float pos[3], const float radius, const float src[3],
+                            const float src_mass, const float G, const float eps2, float out[3])
+{
+    if (law == ORC_LAW_SOFTENED)
+        orc_gravity_softened(pos, src, src_mass, G, eps2, out);
+    else
+        orc_gravity(pos, radius, src, src_mass, G, out);
+}
+
 /* Wrap into [-size/2, size/2]: physics.h:50-58 (double fmod, as the reference writes it). */
 float orc_wrap(const float x, const float size)
 {
@@ -142,6 +170,8 @@ typedef struct
     const int64_t* targets;
     float* acc_out;     /* 3 per target, or NULL to write Body::acc in place */
     float* bodies_rw;
+    int law;
+    float eps2;
 } orc_bf_ctx;
 
 static void orc_bf_block(void* p, const size_t begin, const size_t end)
@@ -158,7 +188,7 @@ static void orc_bf_block(void* p, const size_t begin, const size_t end)
                 continue;
             const float* bj = c->bodies + 12 * j;
             float g[3];
-            orc_gravity(bi, bi[3], bj, bj[7], c->G, g);
+            orc_pair(c->law, bi, bi[3], bj, bj[7], c->G, c->eps2, g);
             acc[0] += g[0];
             acc[1] += g[1];
             acc[2] += g[2];
@@ -174,7 +204,7 @@ void orc_brute_force(float* bodies, const size_t n, const float G, const int nth
 {
     /* Results land in a side buffer first: writing Body::acc in place while other
      * threads read the same bodies is harmless (acc is never read) but keep it simple. */
-    orc_bf_ctx c = { bodies, n, G, NULL, NULL, bodies };
+    orc_bf_ctx c = { bodies, n, G, NULL, NULL, bodies, ORC_LAW_CUTOFF, 0.f };
     orc_parallel(n, nthreads, orc_bf_block, &c);
 }
 
@@ -182,8 +212,15 @@ void orc_brute_force_targets(const float* bodies, const size_t n, const float G,
                              const int64_t* targets, const size_t ntargets, float* acc_out,
                              const int nthreads)
 {
-    orc_bf_ctx c = { bodies, n, G, targets, acc_out, NULL };
-    orc_parallel(ntargets, nthreads, orc_bf_block, &c);
+    orc_brute_force_targets_law(bodies, n, G, ORC_LAW_CUTOFF, 0.f, targets, ntargets, acc_out, nthreads);
+}
+
+void orc_brute_force_targets_law(const float* bodies, const size_t n, const float G, const int law,
+                                 const float eps2, const int64_t* targets, const size_t ntargets,
+                                 float* acc_out, const int nthreads)
+{
+    orc_bf_ctx c = { bodies, n, G, targets, acc_out, NULL, law, eps2 };
+    orc_parallel(targets ? ntargets : n, nthreads, orc_bf_block, &c);
 }
 
 /* ------------------------------------------------------------------------------------
@@ -337,7 +374,61 @@ void orc_tree_insert(orc_tree* t, const float x, const float y, const float z, c
  * bodies inserted in index order. */
 void orc_tree_build(orc_tree* t, const float* bodies, const size_t n, const float size)
 {
-    orc_tree_clear(t, 0.f, 0.f, 0.f, size);
+    orc_tree_build_box(t, bodies, n, 0.f, 0.f, 0.f, size);
+}
+
+/* Replace every node's mass and centre of mass by the exact values over the bodies below
+ * it, summed in double and rounded once to float. No reference counterpart: the reference
+ * keeps an FP32 running mean per node (bhtree.cpp:87-95), whose total mass stalls once it
+ * dwarfs the added masses (16.8M equal bodies lose 6 % of the root mass), while the cells
+ * stay exactly the reference's. A body's path is the insert's descent: the quadrant test
+ * at each split node (bounds.h:31-38), which is where bhtree.cpp:14-85 placed it. */
+int orc_tree_exact_moments(orc_tree* t, const float* bodies, const size_t n)
+{
+    const size_t count = t->count;
+    double* acc = (double*)calloc(4 * (count ? count : 1), sizeof(double));
+    if (!acc)
+        return -1;
+    for (size_t i = 0; i < n; ++i)
+    {
+        const float* b = bodies + 12 * i;
+        const double m = b[7];
+        uint32_t idx = 0;
+        for (;;)
+        {
+            double* a = acc + 4 * idx;
+            a[0] += m;
+            a[1] += m * b[0];
+            a[2] += m * b[1];
+            a[3] += m * b[2];
+            const orc_node* nd = &t->nodes[idx];
+            if (nd->children == 0)
+                break;
+            idx = nd->children + orc_quadrant(nd, b[0], b[1], b[2]);
+        }
+    }
+    for (size_t k = 0; k < count; ++k)
+    {
+        const double* a = acc + 4 * k;
+        orc_node* nd = &t->nodes[k];
+        nd->mass = (float)a[0];
+        if (a[0] != 0.0)
+        {
+            nd->comx = (float)(a[1] / a[0]);
+            nd->comy = (float)(a[2] / a[0]);
+            nd->comz = (float)(a[3] / a[0]);
+        }
+    }
+    free(acc);
+    return 0;
+}
+
+/* The same insertion sequence on a root box of any centre (the reference always centres
+ * its root at the origin, tree.h:20; the device tree may fit a box around the bodies). */
+void orc_tree_build_box(orc_tree* t, const float* bodies, const size_t n, const float cx, const float cy,
+                        const float cz, const float size)
+{
+    orc_tree_clear(t, cx, cy, cz, size);
     for (size_t i = 0; i < n; ++i)
     {
         const float* b = bodies + 12 * i;
@@ -345,7 +436,10 @@ void orc_tree_build(orc_tree* t, const float* bodies, const size_t n, const floa
     }
 }
 
-/* Tree::apply with the gravity visitor: bhtree.cpp:97-138 and cpu_barnes_hut.h:31-41. */
+/* Tree::apply with the gravity visitor: bhtree.cpp:97-138 and cpu_barnes_hut.h:31-41.
+ * The visitor applies the reference's cutoff law, or the softened law with eps2 (the law
+ * of the benchmark configurations); the walk and the opening test are the reference's
+ * either way. */
 typedef struct
 {
     const orc_tree* tree;
@@ -354,6 +448,8 @@ typedef struct
     float theta, G;
     float* acc_out;
     uint64_t* counts;   /* per target interaction counts */
+    int law;
+    float eps2;
 } orc_bh_ctx;
 
 static void orc_bh_block(void* p, const size_t begin, const size_t end)
@@ -391,7 +487,7 @@ static void orc_bh_block(void* p, const size_t begin, const size_t end)
             {
                 const float com[3] = { nd->comx, nd->comy, nd->comz };
                 float g[3];
-                orc_gravity(b, b[3], com, nd->mass, c->G, g);
+                orc_pair(c->law, b, b[3], com, nd->mass, c->G, c->eps2, g);
                 acc[0] += g[0];
                 acc[1] += g[1];
                 acc[2] += g[2];
@@ -411,9 +507,18 @@ void orc_tree_accel(const orc_tree* t, const float* bodies, const size_t n,
                     const int64_t* targets, const size_t ntargets, const float theta,
                     const float G, float* acc_out, uint64_t* interactions, const int nthreads)
 {
+    orc_tree_accel_law(t, bodies, n, targets, ntargets, theta, G, ORC_LAW_CUTOFF, 0.f, acc_out, interactions,
+                       nthreads);
+}
+
+void orc_tree_accel_law(const orc_tree* t, const float* bodies, const size_t n,
+                        const int64_t* targets, const size_t ntargets, const float theta,
+                        const float G, const int law, const float eps2, float* acc_out,
+                        uint64_t* interactions, const int nthreads)
+{
     const size_t nt = targets ? ntargets : n;
     uint64_t* counts = interactions ? (uint64_t*)calloc(nt ? nt : 1, sizeof(uint64_t)) : NULL;
-    orc_bh_ctx c = { t, bodies, targets, theta, G, acc_out, counts };
+    orc_bh_ctx c = { t, bodies, targets, theta, G, acc_out, counts, law, eps2 };
     orc_parallel(nt, nthreads, orc_bh_block, &c);
     if (interactions)
     {
@@ -431,21 +536,37 @@ void orc_nodes_accel(const orc_node* nodes, const size_t count, const float* bod
                      const int64_t* targets, const size_t ntargets, const float theta, const float G,
                      float* acc_out, uint64_t* interactions, const int nthreads)
 {
+    orc_nodes_accel_law(nodes, count, bodies, n, targets, ntargets, theta, G, ORC_LAW_CUTOFF, 0.f, acc_out,
+                        interactions, nthreads);
+}
+
+void orc_nodes_accel_law(const orc_node* nodes, const size_t count, const float* bodies, const size_t n,
+                         const int64_t* targets, const size_t ntargets, const float theta, const float G,
+                         const int law, const float eps2, float* acc_out, uint64_t* interactions,
+                         const int nthreads)
+{
     orc_tree t;
     t.nodes = (orc_node*)nodes;
     t.count = count;
     t.cap = count;
-    orc_tree_accel(&t, bodies, n, targets, ntargets, theta, G, acc_out, interactions, nthreads);
+    orc_tree_accel_law(&t, bodies, n, targets, ntargets, theta, G, law, eps2, acc_out, interactions, nthreads);
 }
 
 /* CpuBarnesHutSolver::accelerate: cpu_barnes_hut.h:22-44 (acc written in place). */
 void orc_barnes_hut(float* bodies, const size_t n, const float size, const float theta,
                     const float G, const int nthreads, uint64_t* interactions)
 {
+    orc_barnes_hut_law(bodies, n, size, theta, G, ORC_LAW_CUTOFF, 0.f, nthreads, interactions);
+}
+
+void orc_barnes_hut_law(float* bodies, const size_t n, const float size, const float theta,
+                        const float G, const int law, const float eps2, const int nthreads,
+                        uint64_t* interactions)
+{
     orc_tree* t = orc_tree_new(size);
     orc_tree_build(t, bodies, n, size);
     float* acc = (float*)malloc(sizeof(float) * 3 * (n ? n : 1));
-    orc_tree_accel(t, bodies, n, NULL, 0, theta, G, acc, interactions, nthreads);
+    orc_tree_accel_law(t, bodies, n, NULL, 0, theta, G, law, eps2, acc, interactions, nthreads);
     for (size_t i = 0; i < n; ++i)
         memcpy(bodies + 12 * i + 8, acc + 3 * i, 3 * sizeof(float));
     free(acc);

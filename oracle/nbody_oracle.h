@@ -56,12 +56,30 @@ void orc_brute_force_targets(const float* bodies, size_t n, float G,
 void orc_barnes_hut(float* bodies, size_t n, float size, float theta, float G,
                     int nthreads, uint64_t* interactions);
 
+/* The softened law G*m*d/(|d|^2 + eps2)^(3/2) in the reference law's operation order
+ * (no cutoff), and the solvers above with the law chosen (ORC_LAW_CUTOFF: the
+ * reference's own). No reference counterpart: the benchmark configurations soften. */
+void orc_gravity_softened(const float pos[3], const float src[3], float src_mass, float G,
+                          float eps2, float out[3]);
+void orc_brute_force_targets_law(const float* bodies, size_t n, float G, int law, float eps2,
+                                 const int64_t* targets, size_t ntargets, float* acc_out,
+                                 int nthreads);
+void orc_barnes_hut_law(float* bodies, size_t n, float size, float theta, float G, int law,
+                        float eps2, int nthreads, uint64_t* interactions);
+
 /* --- octree (source/bhtree.cpp, source/detail/tree.h) ----------------------------- */
 orc_tree* orc_tree_new(float size);
 void orc_tree_free(orc_tree* t);
 void orc_tree_clear(orc_tree* t, float cx, float cy, float cz, float size);
 void orc_tree_insert(orc_tree* t, float x, float y, float z, float mass);
 void orc_tree_build(orc_tree* t, const float* bodies, size_t n, float size);
+/* orc_tree_build on a root box centred at (cx, cy, cz) with edge size. */
+void orc_tree_build_box(orc_tree* t, const float* bodies, size_t n, float cx, float cy, float cz,
+                        float size);
+/* Recompute each node's mass and centre of mass exactly (double sums over its bodies, one
+ * rounding to float), keeping the reference's cells. bodies must be the ones the tree was
+ * built from. Returns 0, or -1 when the scratch cannot be allocated. */
+int orc_tree_exact_moments(orc_tree* t, const float* bodies, size_t n);
 size_t orc_tree_size(const orc_tree* t);
 const orc_node* orc_tree_nodes(const orc_tree* t);
 /* Barnes-Hut acceleration for listed targets (or all bodies when targets is NULL). */
@@ -73,6 +91,16 @@ void orc_tree_accel(const orc_tree* t, const float* bodies, size_t n,
 void orc_nodes_accel(const orc_node* nodes, size_t count, const float* bodies, size_t n,
                      const int64_t* targets, size_t ntargets, float theta, float G,
                      float* acc_out, uint64_t* interactions, int nthreads);
+/* The two walks above with the law chosen (the softened visitor applies
+ * orc_gravity_softened to every accepted node; the walk is unchanged). */
+void orc_tree_accel_law(const orc_tree* t, const float* bodies, size_t n,
+                        const int64_t* targets, size_t ntargets, float theta, float G,
+                        int law, float eps2, float* acc_out, uint64_t* interactions,
+                        int nthreads);
+void orc_nodes_accel_law(const orc_node* nodes, size_t count, const float* bodies, size_t n,
+                         const int64_t* targets, size_t ntargets, float theta, float G,
+                         int law, float eps2, float* acc_out, uint64_t* interactions,
+                         int nthreads);
 
 /* --- FP64 direct sum (no reference counterpart) ----------------------------------- */
 /* pos_mass: 4 floats per body (x, y, z, m). radius: per-body cutoff radius for

@@ -51,12 +51,23 @@ def lib():
         L.orc_brute_force.argtypes = [_F, _SZ, C.c_float, C.c_int]
         L.orc_brute_force_targets.argtypes = [_F, _SZ, C.c_float, _I64, _SZ, _F, C.c_int]
         L.orc_barnes_hut.argtypes = [_F, _SZ, C.c_float, C.c_float, C.c_float, C.c_int, _U64]
+        L.orc_gravity_softened.argtypes = [_F, _F, C.c_float, C.c_float, C.c_float, _F]
+        L.orc_brute_force_targets_law.argtypes = [_F, _SZ, C.c_float, C.c_int, C.c_float, _I64, _SZ, _F, C.c_int]
+        L.orc_barnes_hut_law.argtypes = [_F, _SZ, C.c_float, C.c_float, C.c_float, C.c_int, C.c_float, C.c_int,
+                                         _U64]
+        L.orc_tree_accel_law.argtypes = [C.c_void_p, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, C.c_int, C.c_float,
+                                         _F, _U64, C.c_int]
+        L.orc_nodes_accel_law.argtypes = [C.c_void_p, _SZ, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, C.c_int,
+                                          C.c_float, _F, _U64, C.c_int]
         L.orc_tree_new.argtypes = [C.c_float]
         L.orc_tree_new.restype = C.c_void_p
         L.orc_tree_free.argtypes = [C.c_void_p]
         L.orc_tree_clear.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
         L.orc_tree_insert.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
         L.orc_tree_build.argtypes = [C.c_void_p, _F, _SZ, C.c_float]
+        L.orc_tree_build_box.argtypes = [C.c_void_p, _F, _SZ, C.c_float, C.c_float, C.c_float, C.c_float]
+        L.orc_tree_exact_moments.argtypes = [C.c_void_p, _F, _SZ]
+        L.orc_tree_exact_moments.restype = C.c_int
         L.orc_tree_size.argtypes = [C.c_void_p]
         L.orc_tree_size.restype = _SZ
         L.orc_tree_nodes.argtypes = [C.c_void_p]
@@ -152,19 +163,29 @@ def brute_force(bodies, G, nthreads=0):
     return b
 
 
-def brute_force_targets(bodies, G, targets, nthreads=0):
-    b = _bodies(bodies)
-    t = np.ascontiguousarray(targets, np.int64)
-    out = np.zeros((len(t), 3), np.float32)
-    lib().orc_brute_force_targets(_p(b, _F), len(b), G, _p(t, _I64), len(t), _p(out, _F), nthreads)
+def gravity_softened(pos, src, src_mass, G, eps2):
+    out = np.zeros(3, np.float32)
+    lib().orc_gravity_softened(_p(np.ascontiguousarray(pos, np.float32), _F),
+                               _p(np.ascontiguousarray(src, np.float32), _F), src_mass, G, eps2, _p(out, _F))
     return out
 
 
-def barnes_hut(bodies, size, theta, G, nthreads=0):
-    """CpuBarnesHutSolver::accelerate restated; returns (bodies with acc, interactions)."""
+def brute_force_targets(bodies, G, targets, nthreads=0, law=LAW_CUTOFF, eps2=0.0):
+    """CpuBruteForceSolver::accelerate (cpu_brute_force.h:17-43) for the listed targets, with
+    the reference's cutoff law or the softened law (eps2)."""
+    b = _bodies(bodies)
+    t = np.ascontiguousarray(targets, np.int64)
+    out = np.zeros((len(t), 3), np.float32)
+    lib().orc_brute_force_targets_law(_p(b, _F), len(b), G, law, eps2, _p(t, _I64), len(t), _p(out, _F), nthreads)
+    return out
+
+
+def barnes_hut(bodies, size, theta, G, nthreads=0, law=LAW_CUTOFF, eps2=0.0):
+    """CpuBarnesHutSolver::accelerate restated; returns (bodies with acc, interactions).
+    law/eps2 choose the visitor's force law (the reference's cutoff law by default)."""
     b = _bodies(bodies).copy()
     inter = np.zeros(1, np.uint64)
-    lib().orc_barnes_hut(_p(b, _F), len(b), size, theta, G, nthreads, _p(inter, _U64))
+    lib().orc_barnes_hut_law(_p(b, _F), len(b), size, theta, G, law, eps2, nthreads, _p(inter, _U64))
     return b, int(inter[0])
 
 
@@ -187,20 +208,38 @@ class Tree:
         b = _bodies(bodies)
         lib().orc_tree_build(self._t, _p(b, _F), len(b), size)
 
+    def build_on_box(self, bodies, box):
+        """Insert every body, in index order, under a root box given as (lower corner xyz,
+        edge), as the device tree's root box is reported (nbody_cuda_morton)."""
+        b = _bodies(bodies)
+        e = float(box[3])
+        lib().orc_tree_build_box(self._t, _p(b, _F), len(b), float(box[0]) + 0.5 * e, float(box[1]) + 0.5 * e,
+                                 float(box[2]) + 0.5 * e, e)
+
+    def exact_moments(self, bodies):
+        """Replace every node's mass and centre of mass by exact (FP64-summed) values over
+        its bodies, keeping the reference's cells: the reference tree without the FP32
+        running mean's drift (bhtree.cpp:87-95)."""
+        b = _bodies(bodies)
+        if lib().orc_tree_exact_moments(self._t, _p(b, _F), len(b)) != 0:
+            raise MemoryError("orc_tree_exact_moments: no scratch")
+
     def nodes(self):
         n = lib().orc_tree_size(self._t)
         ptr = lib().orc_tree_nodes(self._t)
         buf = (C.c_char * (48 * n)).from_address(ptr)
         return np.frombuffer(bytes(buf), dtype=NODE_DTYPE).copy()
 
-    def accel(self, bodies, theta, G, targets=None, nthreads=0):
+    def accel(self, bodies, theta, G, targets=None, nthreads=0, law=LAW_CUTOFF, eps2=0.0):
+        """Tree::apply (bhtree.cpp:97-138) with the gravity visitor of cpu_barnes_hut.h:31-41
+        for the listed targets; law/eps2 choose the visitor's force law."""
         b = _bodies(bodies)
         t = None if targets is None else np.ascontiguousarray(targets, np.int64)
         nt = len(b) if t is None else len(t)
         out = np.zeros((nt, 3), np.float32)
         inter = np.zeros(1, np.uint64)
-        lib().orc_tree_accel(self._t, _p(b, _F), len(b), _p(t, _I64), 0 if t is None else len(t),
-                             theta, G, _p(out, _F), _p(inter, _U64), nthreads)
+        lib().orc_tree_accel_law(self._t, _p(b, _F), len(b), _p(t, _I64), 0 if t is None else len(t),
+                                 theta, G, law, eps2, _p(out, _F), _p(inter, _U64), nthreads)
         return out, int(inter[0])
 
 
@@ -211,7 +250,7 @@ def tree_nodes(bodies, size):
     return t.nodes()
 
 
-def nodes_accel(nodes, bodies, theta, G, targets=None, nthreads=0):
+def nodes_accel(nodes, bodies, theta, G, targets=None, nthreads=0, law=LAW_CUTOFF, eps2=0.0):
     """Tree::apply (bhtree.cpp:97-138) over a node array in the reference layout."""
     nd = np.ascontiguousarray(nodes)
     assert nd.dtype == NODE_DTYPE
@@ -220,8 +259,9 @@ def nodes_accel(nodes, bodies, theta, G, targets=None, nthreads=0):
     nt = len(b) if t is None else len(t)
     out = np.zeros((nt, 3), np.float32)
     inter = np.zeros(1, np.uint64)
-    lib().orc_nodes_accel(nd.ctypes.data_as(C.c_void_p), len(nd), _p(b, _F), len(b), _p(t, _I64),
-                          0 if t is None else len(t), theta, G, _p(out, _F), _p(inter, _U64), nthreads)
+    lib().orc_nodes_accel_law(nd.ctypes.data_as(C.c_void_p), len(nd), _p(b, _F), len(b), _p(t, _I64),
+                              0 if t is None else len(t), theta, G, law, eps2, _p(out, _F), _p(inter, _U64),
+                              nthreads)
     return out, int(inter[0])
 
 

@@ -119,6 +119,73 @@ def test_theta_convention_accuracy():
     assert ti > li > 0 and ti < 100 * 100
 
 
+# --- the softened law (the benchmark configurations' law; no reference counterpart) ------------
+
+def test_softened_pair_against_fp64():
+    """orc_gravity_softened is G*m*d/(|d|^2 + eps2)^(3/2) to FP32 rounding."""
+    g = np.random.default_rng(21)
+    for _ in range(200):
+        x, s = g.normal(0, 1, 3).astype(np.float32), g.normal(0, 1, 3).astype(np.float32)
+        m, eps2 = np.float32(g.uniform(0.1, 2)), np.float32(10.0 ** g.uniform(-6, 0))
+        got = O.gravity_softened(x, s, m, 1.5, eps2)
+        d = s.astype(np.float64) - x
+        want = 1.5 * float(m) * d / (d @ d + float(eps2)) ** 1.5
+        assert np.linalg.norm(got - want) <= 4e-7 * np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("fixture", ["disk_1024.npz", "cube_4096.npz"])
+def test_softened_visitor_at_vanishing_eps_is_the_reference_walk(fixture):
+    """The softened visitor follows the reference's walk and opening test unchanged: with
+    eps2 far below every |d|^2 (and radii 0, so the cutoff only drops d = 0) it adds exactly
+    the terms of the reference-law walk, which the fixtures pin to the reference bit for
+    bit, and so gives the same bits and the same interaction count."""
+    b = golden(fixture)["bodies"].copy()
+    b[:, 3] = 0.0
+    t = O.Tree(10000.0)
+    t.build(b, 10000.0)
+    for theta in (0.5, 2.0):
+        ref, ri = t.accel(b, theta, 1.0)
+        soft, si = t.accel(b, theta, 1.0, law=O.LAW_SOFTENED, eps2=1e-30)
+        assert si == ri
+        assert np.array_equal(soft.view(np.uint32), ref.view(np.uint32))
+    bh, _ = O.barnes_hut(b, 10000.0, 0.5, 1.0, law=O.LAW_SOFTENED, eps2=1e-30)
+    assert np.array_equal(bh[:, 8:11], t.accel(b, 0.5, 1.0)[0])
+
+
+def test_softened_brute_force_against_fp64():
+    """The softened brute force (the reference's loop, cpu_brute_force.h:17-43, with the
+    softened pair) sits within FP32 summation error of the FP64 softened sum."""
+    from nbody_gb300 import scenes
+    b = scenes.plummer(2048, seed=77)
+    eps2 = 1e-4
+    tg = np.arange(0, 2048, 7)
+    a = O.brute_force_targets(b, 1.0, tg, law=O.LAW_SOFTENED, eps2=eps2)
+    a64, scale = O.direct_f64(b[:, [0, 1, 2, 7]], 1.0, float(np.float32(eps2)), O.LAW_SOFTENED, targets=tg,
+                              with_scale=True)
+    err = np.linalg.norm(a - a64, axis=1) / scale
+    assert err.max() < 5e-6 and np.median(err) < 1e-6
+
+
+def test_softened_theta_convention_accuracy():
+    """test_bhtree.cpp:259-367 with the softened visitor (eps = 1 on a 100-unit cloud):
+    reference theta 8 is accurate (< 0.05 of the mean force), 0.5 loose (< 3.0)."""
+    g = np.random.default_rng(11)
+    p = np.clip(g.normal(0, 0.5, (100, 3)), -1, 1).astype(np.float32) * 100
+    b = np.zeros((100, 12), np.float32)
+    b[:, :3] = p
+    b[:, 7] = 1
+    exact = O.direct_f64(b[:, [0, 1, 2, 7]], 1.0, 1.0, O.LAW_SOFTENED)
+    mean_force = np.linalg.norm(exact, axis=1).mean()
+    t = O.Tree(200.0)
+    t.build(b, 200.0)
+    loose, li = t.accel(b, 0.5, 1.0, law=O.LAW_SOFTENED, eps2=1.0)
+    tight, ti = t.accel(b, 8.0, 1.0, law=O.LAW_SOFTENED, eps2=1.0)
+    el = np.linalg.norm(loose - exact, axis=1).max() / mean_force
+    et = np.linalg.norm(tight - exact, axis=1).max() / mean_force
+    assert et < el and et < 0.05 and el < 3.0
+    assert ti > li > 0
+
+
 # --- bit-for-bit against the reference's own outputs ---------------------------------------
 
 @pytest.mark.parametrize("n", [512, 1024, 2048])
