@@ -75,6 +75,21 @@ typedef enum nbody_precision
     NBODY_PREC_FP64 = 2
 } nbody_precision;
 
+/* Barnes-Hut traversal (nbody_step_params.walk). No reference counterpart beyond TARGET. */
+typedef enum nbody_walk
+{
+    NBODY_WALK_TARGET = 0,      /* every target decides every cell itself with the reference's
+                                   opening test, and applies exactly the cells the reference's
+                                   walk accepts for it (bhtree.cpp:97-138) */
+    NBODY_WALK_GROUP = 1        /* one walk per group of Morton-consecutive targets: a cell is
+                                   accepted for the whole group when the group's bounding box
+                                   lies beyond the cell's opening distance, and the accepted
+                                   cells and leaves form an interaction list applied to every
+                                   target of the group. Each target's sum refines the set the
+                                   reference accepts for it (at least as accurate, more
+                                   interactions, far fewer instructions per interaction) */
+} nbody_walk;
+
 /* Device-side body layout of a context: the reference's two GPU layouts. */
 typedef enum nbody_layout
 {
@@ -109,7 +124,8 @@ typedef struct nbody_step_params
                            with edge `size` (source/detail/tree.h:20); 1 = the smallest
                            power-of-two cube around the bodies (FP64 bounding box).
                            0 with size <= 0 behaves as 1. */
-    int32_t reserved[2];/* zero */
+    int32_t walk;       /* nbody_walk (Barnes-Hut only); zero is the reference's per-target walk */
+    int32_t reserved;   /* zero */
 } nbody_step_params;
 
 typedef struct nbody_cuda nbody_cuda;

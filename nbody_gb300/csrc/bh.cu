@@ -56,6 +56,13 @@ namespace nbg
         // lane masks, and the stacks of one CTA stay within 48 KB of static shared memory
         __host__ __device__ constexpr int pair_warps(const int q) { return q > 2 ? 4 : kTravWarps; }
         constexpr int kStack = 192;
+        // group walk: warps per CTA, list entries and stacked parent cells per warp (the
+        // stack grows by at most 28 parents per tree level, 22 levels: 616 < 768)
+        constexpr int kListWarps = 4;
+        constexpr int kListCap = 256;       // full-list entries
+        constexpr int kPartCap = 128;       // partial-list entries
+        constexpr int kGroupStack = 768;
+        constexpr int kSubGroups = 4;       // sub-groups per group (a 4-bit mask per stacked cell)
         constexpr int kBboxBlocks = 1024;
         constexpr int kBboxVals = 8;    // min x y z, max x y z, max |m|, max |x|
         constexpr int kMomThreads = 1024;
@@ -1118,6 +1125,424 @@ namespace nbg
     }
 
     // ------------------------------------------------------------------------------------
+    // 7b. group walk with interaction lists (walk = NBODY_WALK_GROUP)
+    // ------------------------------------------------------------------------------------
+    // One list source applied to two targets (negated positions): the direct sum's packed
+    // interaction, 3 FADD2 + 3 FFMA2 + 2 MUFU.RSQ + 3 FMUL2 + 3 FFMA2. MASKED: a half
+    // whose target does not take the source gets s = 0, which adds exactly zero.
+    template <int LAW, bool MASKED>
+    __device__ __forceinline__ void apply_list2(const float2 npx, const float2 npy, const float2 npz, const float2 lim,
+                                                const float4 s, const bool take_a, const bool take_b, float2& ax,
+                                                float2& ay, float2& az)
+    {
+        const float2 dx = add2(f2(s.x), npx), dy = add2(f2(s.y), npy), dz = add2(f2(s.z), npz);
+        float2 r2 = (LAW == NBODY_LAW_SOFTENED) ? fma2(dx, dx, lim) : mul2(dx, dx);
+        r2 = fma2(dy, dy, r2);
+        r2 = fma2(dz, dz, r2);
+        float2 inv = make_float2(rsqrt_sfu(r2.x), rsqrt_sfu(r2.y));
+        if (LAW == NBODY_LAW_CUTOFF)
+        {
+            inv.x = r2.x > lim.x ? inv.x : 0.f;     // physics.h:38-39
+            inv.y = r2.y > lim.y ? inv.y : 0.f;
+        }
+        const float2 inv2 = mul2(inv, inv);
+        const float2 mi = mul2(f2(s.w), inv);
+        float2 sc = mul2(mi, inv2);
+        if (MASKED)
+        {
+            sc.x = take_a ? sc.x : 0.f;
+            sc.y = take_b ? sc.y : 0.f;
+        }
+        ax = fma2(dx, sc, ax);
+        ay = fma2(dy, sc, ay);
+        az = fma2(dz, sc, az);
+    }
+
+    // The reference's opening test (bhtree.cpp:117-125) for a box of targets: the cell is
+    // accepted when the nearest point of the box lies beyond its opening distance,
+    // |com - p|^2 > size^2 * theta^2. Every target in the box is at least that far from the
+    // centre of mass, so each would accept the cell itself.
+    __device__ __forceinline__ bool box_accepts(const float4 cm, const float open_r2, const float4 lo, const float4 hi)
+    {
+        const float dx = fmaxf(fmaxf(lo.x - cm.x, cm.x - hi.x), 0.f);
+        const float dy = fmaxf(fmaxf(lo.y - cm.y, cm.y - hi.y), 0.f);
+        const float dz = fmaxf(fmaxf(lo.z - cm.z, cm.z - hi.z), 0.f);
+        return fmaf(dz, dz, fmaf(dy, dy, dx * dx)) > open_r2;
+    }
+
+    // A warp serves 64 Q Morton-consecutive targets (lane l holds targets 64 Q t + 32 h + l,
+    // h < 2Q, as Q packed pairs) with one walk of the tree, the interaction-list walk of GPU
+    // tree codes (Barnes 1990's grouping; Bonsai, Bedorf et al. 2012).
+    //
+    // Sub-groups. The targets are split at the kSubGroups - 1 largest jumps of their Morton
+    // codes (the smallest common prefixes of neighbours) into sub-groups, each with its own
+    // bounding box: a run that crosses from one cell of the tree into a distant one (at the
+    // end of a top-level octant the curve jumps across the whole system) would otherwise
+    // have a box spanning everything between, and open every cell there down to its leaves.
+    //
+    // The walk decides each cell once per sub-group and appends the sources it yields --
+    // accepted cells as (com, mass), leaves and the bodies of opened buckets as (x, m) --
+    // to an interaction list in shared memory, with the sub-groups that take each source.
+    // Sources every sub-group takes go to a full list, applied to every target with the
+    // direct sum's packed loop; the rest go to a partial list applied with a per-target
+    // selection. Both are drained when either fills.
+    //
+    // The walk tests up to 32 cells at a time: it pops up to four parent cells, each with
+    // the sub-groups that opened it, from a stack, and lane l tests child l % 8 of parent
+    // l / 8. The stack grows by at most 28 parents per tree level (22 levels: 616 < 768).
+    //
+    // Each target's sources refine the cells the reference's walk accepts for it alone (a
+    // cell opened for its sub-group may be one the target would have accepted), so each
+    // target is summed at least as finely as in the reference, over more interactions.
+    template <int LAW, int Q>
+    __global__ void __launch_bounds__(kListWarps * 32) traverse_list_kernel(
+        const OctNode* __restrict__ nodes, const float4* __restrict__ spm, const float* __restrict__ srad,
+        const uint64_t* __restrict__ codes, const uint32_t* __restrict__ order, const int n, const float G,
+        const float eps2, float4* __restrict__ acc, float* __restrict__ body_out, unsigned* __restrict__ err,
+        unsigned long long* __restrict__ stats)
+    {
+        constexpr int H = 2 * Q;                    // target slots per lane
+        constexpr int TW = 32 * H;                  // targets per group
+        constexpr int NSG = kSubGroups;
+        __shared__ __align__(16) float4 full_mem[kListWarps][kListCap];
+        __shared__ __align__(16) float4 part_mem[kListWarps][kPartCap];
+        __shared__ unsigned char pmask_mem[kListWarps][kPartCap];
+        __shared__ unsigned stack_mem[kListWarps][kGroupStack];   // cell | sub-group mask << 28
+        __shared__ __align__(16) float4 box_mem[kListWarps][2 * NSG];
+        __shared__ int cnt_mem[kListWarps][1 << NSG];            // valid targets per sub-group mask
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const unsigned lt = (1u << lane) - 1u;
+        float4* full = full_mem[warp];
+        float4* part = part_mem[warp];
+        unsigned char* pmask = pmask_mem[warp];
+        unsigned* stk = stack_mem[warp];
+        const float4* box = box_mem[warp];
+        const int* cnt_of = cnt_mem[warp];
+        unsigned long long inter = 0;               // interactions summed by this warp (uniform)
+        unsigned iters = 0;
+
+        auto next_tile = [&]() {
+            unsigned long long t = 0;
+            if (lane == 0)
+                t = atomicAdd(&stats[3], 1ull);
+            return static_cast<int>(__shfl_sync(0xffffffffu, t, 0));
+        };
+        for (int tile = next_tile(); static_cast<long long>(tile) * TW < n; tile = next_tile())
+        {
+            const int t0 = tile * TW;
+            // --- sub-group splits: the NSG - 1 largest Morton jumps between neighbours ---
+            unsigned key[H];    // (common prefix bits << 8 | position); 0xffffffff: no boundary
+#pragma unroll
+            for (int h = 0; h < H; ++h)
+            {
+                const int b = 32 * h + lane;        // boundary between positions b - 1 and b
+                key[h] = 0xffffffffu;
+                if (b > 0 && t0 + b < n)
+                    key[h] = (static_cast<unsigned>(__clzll(static_cast<long long>(codes[t0 + b - 1] ^ codes[t0 + b])))
+                              << 8) | static_cast<unsigned>(b);
+            }
+            int split[NSG - 1];
+#pragma unroll
+            for (int sidx = 0; sidx < NSG - 1; ++sidx)
+            {
+                unsigned m = key[0];
+#pragma unroll
+                for (int h = 1; h < H; ++h)
+                    m = min(m, key[h]);
+                for (int o = 16; o > 0; o >>= 1)
+                    m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+                split[sidx] = m == 0xffffffffu ? TW : static_cast<int>(m & 0xffu);
+#pragma unroll
+                for (int h = 0; h < H; ++h)
+                    if (key[h] == m)
+                        key[h] = 0xffffffffu;
+            }
+            // --- targets, their sub-group bits and the sub-group boxes ---
+            float2 npx[Q], npy[Q], npz[Q], lim[Q], ax[Q], ay[Q], az[Q];
+            unsigned bit[H];
+            float4 blo[NSG], bhi[NSG];
+#pragma unroll
+            for (int g = 0; g < NSG; ++g)
+            {
+                blo[g] = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
+                bhi[g] = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+            }
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+            {
+                float v[2][4];
+#pragma unroll
+                for (int e = 0; e < 2; ++e)
+                {
+                    const int h = 2 * q + e;
+                    const int pos = 32 * h + lane;
+                    const int k = t0 + pos;
+                    const bool valid = k < n;
+                    int sg = 0;
+#pragma unroll
+                    for (int sidx = 0; sidx < NSG - 1; ++sidx)
+                        sg += pos >= split[sidx] ? 1 : 0;
+                    bit[h] = valid ? (1u << sg) : 0u;
+                    const float4 pk = spm[valid ? k : n - 1];
+#pragma unroll
+                    for (int g = 0; g < NSG; ++g)
+                        if (valid && sg == g)
+                        {
+                            blo[g] = make_float4(fminf(blo[g].x, pk.x), fminf(blo[g].y, pk.y), fminf(blo[g].z, pk.z), 0.f);
+                            bhi[g] = make_float4(fmaxf(bhi[g].x, pk.x), fmaxf(bhi[g].y, pk.y), fmaxf(bhi[g].z, pk.z), 0.f);
+                        }
+                    v[e][0] = -pk.x;
+                    v[e][1] = -pk.y;
+                    v[e][2] = -pk.z;
+                    if (LAW == NBODY_LAW_CUTOFF)
+                    {
+                        const float r = srad[valid ? k : n - 1];
+                        v[e][3] = r * r;
+                    }
+                    else
+                        v[e][3] = eps2;
+                }
+                npx[q] = make_float2(v[0][0], v[1][0]);
+                npy[q] = make_float2(v[0][1], v[1][1]);
+                npz[q] = make_float2(v[0][2], v[1][2]);
+                lim[q] = make_float2(v[0][3], v[1][3]);
+                ax[q] = ay[q] = az[q] = make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int g = 0; g < NSG; ++g)
+                for (int o = 16; o > 0; o >>= 1)
+                {
+                    blo[g].x = fminf(blo[g].x, __shfl_xor_sync(0xffffffffu, blo[g].x, o));
+                    blo[g].y = fminf(blo[g].y, __shfl_xor_sync(0xffffffffu, blo[g].y, o));
+                    blo[g].z = fminf(blo[g].z, __shfl_xor_sync(0xffffffffu, blo[g].z, o));
+                    bhi[g].x = fmaxf(bhi[g].x, __shfl_xor_sync(0xffffffffu, bhi[g].x, o));
+                    bhi[g].y = fmaxf(bhi[g].y, __shfl_xor_sync(0xffffffffu, bhi[g].y, o));
+                    bhi[g].z = fmaxf(bhi[g].z, __shfl_xor_sync(0xffffffffu, bhi[g].z, o));
+                }
+            // valid targets per sub-group, and the sub-groups that have any (the full mask)
+            int cnt[NSG];
+#pragma unroll
+            for (int g = 0; g < NSG; ++g)
+            {
+                cnt[g] = 0;
+#pragma unroll
+                for (int h = 0; h < H; ++h)
+                    cnt[g] += __popc(__ballot_sync(0xffffffffu, bit[h] == (1u << g)));
+            }
+            unsigned all = 0;
+#pragma unroll
+            for (int g = 0; g < NSG; ++g)
+                all |= cnt[g] > 0 ? (1u << g) : 0u;
+            __syncwarp();       // the previous group's readers of box/cnt are done
+            if (lane < 2 * NSG)
+            {
+                const int g = lane >> 1;
+                float4 bv = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int gg = 0; gg < NSG; ++gg)
+                    if (gg == g)
+                        bv = (lane & 1) ? bhi[gg] : blo[gg];
+                box_mem[warp][lane] = bv;
+            }
+            if (lane < (1 << NSG))
+            {
+                int c = 0;
+#pragma unroll
+                for (int g = 0; g < NSG; ++g)
+                    c += ((lane >> g) & 1) ? cnt[g] : 0;
+                cnt_mem[warp][lane] = c;
+            }
+            __syncwarp();
+
+            int fn_ = 0, pn = 0;    // entries in the full and partial lists (warp-uniform)
+            // apply both lists to every target of the group, then empty them
+            auto drain = [&]() {
+                __syncwarp();
+#pragma unroll 2
+                for (int e = 0; e < fn_; ++e)
+                {
+                    const float4 s = full[e];
+#pragma unroll
+                    for (int q = 0; q < Q; ++q)
+                        apply_list2<LAW, false>(npx[q], npy[q], npz[q], lim[q], s, true, true, ax[q], ay[q], az[q]);
+                }
+                inter += static_cast<unsigned long long>(fn_) * cnt_of[all];
+                for (int e = 0; e < pn; ++e)
+                {
+                    const float4 s = part[e];
+                    const unsigned m = pmask[e];
+#pragma unroll
+                    for (int q = 0; q < Q; ++q)
+                        apply_list2<LAW, true>(npx[q], npy[q], npz[q], lim[q], s, (m & bit[2 * q]) != 0u,
+                                               (m & bit[2 * q + 1]) != 0u, ax[q], ay[q], az[q]);
+                    inter += static_cast<unsigned long long>(cnt_of[m]);
+                }
+                fn_ = 0;
+                pn = 0;
+                __syncwarp();
+            };
+            // append one source per flagged lane (mask: the sub-groups taking it; 0: none),
+            // draining first when a list would overflow
+            auto append = [&](const unsigned mask, const float4 src) {
+                const bool to_full = mask != 0u && mask == all;
+                const bool to_part = mask != 0u && mask != all;
+                const unsigned mf = __ballot_sync(0xffffffffu, to_full);
+                const unsigned mp = __ballot_sync(0xffffffffu, to_part);
+                if (fn_ + __popc(mf) > kListCap || pn + __popc(mp) > kPartCap)
+                    drain();
+                if (to_full)
+                    full[fn_ + __popc(mf & lt)] = src;
+                if (to_part)
+                {
+                    const int at = pn + __popc(mp & lt);
+                    part[at] = src;
+                    pmask[at] = static_cast<unsigned char>(mask);
+                }
+                fn_ += __popc(mf);
+                pn += __popc(mp);
+            };
+            // the bodies of an opened bucket (identical codes), 32 at a time
+            auto append_range = [&](const int first, const int last, const unsigned mask) {
+                for (int b0 = first; b0 <= last; b0 += 32)
+                {
+                    const int bi = b0 + lane;
+                    float4 sb = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (bi <= last)
+                        sb = spm[bi];
+                    append(bi <= last && sb.w != 0.f ? mask : 0u, sb);
+                }
+            };
+            // which of the sub-groups in `mask` accept a cell
+            auto accepting = [&](const float4 cm, const float open_r2, const unsigned mask) {
+                unsigned a = 0;
+#pragma unroll
+                for (int g = 0; g < NSG; ++g)
+                    if (((mask >> g) & 1u) && box_accepts(cm, open_r2, box[2 * g], box[2 * g + 1]))
+                        a |= 1u << g;
+                return a;
+            };
+
+            // the root: accepted, a bucket, or the first parent on the stack
+            int sp = 0;
+            {
+                const float4 cm = nodes[0].com_mass;
+                const int4 meta = *reinterpret_cast<const int4*>(&nodes[0].open_r2);
+                if (cm.w != 0.f)
+                {
+                    const unsigned a = accepting(cm, __int_as_float(meta.x), all);
+                    const unsigned o = all & ~a;
+                    append(lane == 0 ? a : 0u, cm);
+                    if (o && meta.y < 0)
+                        append_range(meta.z, meta.w, o);
+                    else if (o)
+                    {
+                        if (lane == 0)
+                            stk[0] = o << 28;
+                        sp = 1;
+                    }
+                }
+            }
+            __syncwarp();
+            // Each cell is pushed at most once per group, so the walk takes at most one
+            // round per cell (< n); the bound only trips on a malformed tree.
+            int guard = 0;
+            const int guard_limit = n + 64;
+            while (sp > 0)
+            {
+                if (++guard > guard_limit)
+                {
+                    if (lane == 0)
+                        atomicOr(err, DEV_ERR_BOUNDS);
+                    break;
+                }
+                ++iters;
+                const int k = min(sp, 4);
+                const int slot = lane >> 3;
+                int c = 0;              // 0: no child (cell 0 is the root, never a child)
+                unsigned open = 0;      // the sub-groups that opened the parent
+                if (slot < k)
+                {
+                    const unsigned e = stk[sp - 1 - slot];
+                    open = e >> 28;
+                    c = nodes[e & 0x0fffffffu].child[lane & 7];
+                }
+                __syncwarp();           // every parent read before pushes overwrite its slot
+                sp -= k;
+                unsigned take = 0, push = 0, bucket = 0;
+                float4 src = make_float4(0.f, 0.f, 0.f, 0.f);
+                int4 meta = make_int4(0, 0, 0, 0);
+                if (c < 0)
+                {
+                    src = spm[~c];      // a leaf: always applied (bhtree.cpp:115-116)
+                    take = src.w != 0.f ? open : 0u;
+                }
+                else if (c > 0)
+                {
+                    const float4 cm = nodes[c].com_mass;
+                    meta = *reinterpret_cast<const int4*>(&nodes[c].open_r2);
+                    if (cm.w != 0.f)    // empty cells are skipped (bhtree.cpp:109-113)
+                    {
+                        take = accepting(cm, __int_as_float(meta.x), open);
+                        src = cm;
+                        const unsigned o = open & ~take;
+                        if (o && meta.y < 0)
+                            bucket = o;
+                        else
+                            push = o;
+                    }
+                }
+                append(take, src);
+                const unsigned pm = __ballot_sync(0xffffffffu, push != 0u);
+                if (push)
+                {
+                    const int at = sp + __popc(pm & lt);
+                    if (at < kGroupStack)
+                        stk[at] = static_cast<unsigned>(c) | (push << 28);
+                    else
+                        atomicOr(err, DEV_ERR_BOUNDS);
+                }
+                sp = min(kGroupStack, sp + __popc(pm));
+                unsigned bm = __ballot_sync(0xffffffffu, bucket != 0u);
+                while (bm)
+                {
+                    const int bl = __ffs(bm) - 1;
+                    bm &= bm - 1;
+                    append_range(__shfl_sync(0xffffffffu, meta.z, bl), __shfl_sync(0xffffffffu, meta.w, bl),
+                                 __shfl_sync(0xffffffffu, bucket, bl));
+                }
+                __syncwarp();
+            }
+            drain();
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+#pragma unroll
+                for (int e = 0; e < 2; ++e)
+                {
+                    const int k = t0 + (2 * q + e) * 32 + lane;
+                    if (k >= n)
+                        continue;
+                    const uint32_t i = order[k];
+                    const float gx = G * (e ? ax[q].y : ax[q].x), gy = G * (e ? ay[q].y : ay[q].x);
+                    const float gz = G * (e ? az[q].y : az[q].x);
+                    if (body_out)
+                    {
+                        float* o = body_out + static_cast<size_t>(i) * 12 + 8;
+                        o[0] = gx;
+                        o[1] = gy;
+                        o[2] = gz;
+                    }
+                    else
+                        acc[i] = make_float4(gx, gy, gz, 0.f);
+                }
+        }
+        if (lane == 0)
+        {
+            atomicAdd(&stats[0], inter);
+            atomicAdd(&stats[1], static_cast<unsigned long long>(iters));
+        }
+    }
+
+    // ------------------------------------------------------------------------------------
     // host side
     // ------------------------------------------------------------------------------------
     namespace
@@ -1308,6 +1733,41 @@ namespace nbg
         }
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        if (p->walk == NBODY_WALK_GROUP)
+        {
+            // Group walk: 128 targets per group (4 per lane) while the groups outnumber the
+            // resident warps, else 64. NBODY_CUDA_BH_GROUP (64, 128 or 256) overrides; the
+            // group size changes which cells each target applies, not the bar they meet.
+            if (ni >= (1 << 28))
+                return ctx_fail(ctx, NBODY_ERR_UNSUPPORTED, "the group walk takes fewer than 2^28 bodies");
+            const bool soft = p->law == NBODY_LAW_SOFTENED;
+            using Walk = void (*)(const OctNode*, const float4*, const float*, const uint64_t*, const uint32_t*, int,
+                                  float, float, float4*, float*, unsigned*, unsigned long long*);
+            Walk f64 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 1> : traverse_list_kernel<NBODY_LAW_CUTOFF, 1>;
+            Walk f128 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 2> : traverse_list_kernel<NBODY_LAW_CUTOFF, 2>;
+            Walk f256 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 4> : traverse_list_kernel<NBODY_LAW_CUTOFF, 4>;
+            auto per_sm = [&](Walk fn) {
+                int per = 0;
+                if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kListWarps * 32, 0) != cudaSuccess || per < 1)
+                    per = 1;
+                return per;
+            };
+            const char* gsel = std::getenv("NBODY_CUDA_BH_GROUP");
+            int group = gsel ? std::atoi(gsel) : 0;
+            if (group != 64 && group != 128 && group != 256)
+                group = static_cast<long long>(ni) >= 128LL * per_sm(f128) * sms * kListWarps ? 128 : 64;
+            const Walk fn = group == 256 ? f256 : (group == 128 ? f128 : f64);
+            const int per = per_sm(fn);
+            const int groups = (ni + group - 1) / group;
+            const int grid = std::min((groups + kListWarps - 1) / kListWarps, sms * per);
+            fn<<<grid, kListWarps * 32, 0, s>>>(b.nodes, b.spm, b.srad, b.codes, b.order, ni, p->G, p->eps2, acc,
+                                                body_out, ctx->dev_error, b.stats);
+            ++ctx->launches;
+            if (timed)
+                b.timed = cudaEventRecord(b.ev[2], s) == cudaSuccess;
+            const cudaError_t eg = cudaGetLastError();
+            return eg == cudaSuccess ? NBODY_OK : ctx_cuda_fail(ctx, eg, "group tree walk");
+        }
         // Targets per warp walk: 128 (traverse_pairs_kernel, 4 per lane) while the tiles
         // outnumber the resident warps, then 64 (2 per lane) while they are at least half of
         // them, then 32 (traverse_kernel): a narrower walk visits more cells but keeps more

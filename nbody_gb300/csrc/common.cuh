@@ -125,5 +125,21 @@ namespace nbg
     // again, and fma(a, a, +0) rounds exactly as the product a*a (a*a is never -0).
     __device__ __forceinline__ float2 sq2(const float2 a) { return __ffma2_rn(a, a, make_float2(0.f, 0.f)); }
 
+    // a - b per half (the negation is exact, so this is the correctly rounded difference).
+    __device__ __forceinline__ float2 sub2(const float2 a, const float2 b)
+    {
+        return __fadd2_rn(a, make_float2(-b.x, -b.y));
+    }
+
+    // Error-free transformation of a sum (Knuth's TwoSum), per half: s = fl(a + b) and
+    // e = (a + b) - s exactly, for any a and b (no ordering of magnitudes needed). Six
+    // additions, none of which may be reassociated; packed adds are never contracted.
+    __device__ __forceinline__ void two_sum2(const float2 a, const float2 b, float2& s, float2& e)
+    {
+        s = add2(a, b);
+        const float2 bb = sub2(s, a);
+        e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+    }
+
     inline unsigned ceil_div(const size_t a, const size_t b) { return static_cast<unsigned>((a + b - 1) / b); }
 }

@@ -80,6 +80,8 @@ namespace
             return fail(ctx, NBODY_ERR_INVALID, "unknown mode %d", p->mode);
         if (p->precision < NBODY_PREC_FP32 || p->precision > NBODY_PREC_FP64)
             return fail(ctx, NBODY_ERR_INVALID, "unknown precision %d", p->precision);
+        if (p->walk != NBODY_WALK_TARGET && p->walk != NBODY_WALK_GROUP)
+            return fail(ctx, NBODY_ERR_INVALID, "unknown Barnes-Hut walk %d", p->walk);
         return NBODY_OK;
     }
 }
@@ -529,7 +531,7 @@ namespace
         DirectPlan plan = plan_direct(ctx->count, p->law, aos, ctx->force_variant);
         ctx->last_plan = plan;
         if (plan.jsplit > 1)
-            if (const int st = ensure_scratch(ctx, static_cast<size_t>(plan.jsplit) * n * sizeof(float4)))
+            if (const int st = ensure_scratch(ctx, direct_scratch_bytes(plan, ctx->count)))
                 return st;
         const float4* src = aos ? reinterpret_cast<const float4*>(ctx->bodies) : ctx->pm;
         float4* scratch = static_cast<float4*>(ctx->scratch);
@@ -541,6 +543,7 @@ namespace
             if (e != cudaSuccess)
                 return cuda_fail(ctx, e, "direct-sum launch");
             ctx->pending_partials = plan.jsplit;
+            ctx->pending_G = p->G;
             return NBODY_OK;
         }
         ctx->pending_partials = 0;
@@ -559,10 +562,11 @@ namespace
         ctx->pending_partials = 0;
         cudaError_t e;
         if (ctx->layout == NBODY_LAYOUT_SOA)
-            e = launch_integrate_soa(ctx->pm, ctx->vr, ctx->acc, part, js, n, p->dt, p->size, p->wrap, ctx->stream,
-                                     &ctx->launches);
+            e = launch_integrate_soa(ctx->pm, ctx->vr, ctx->acc, part, js, n, ctx->pending_G, p->dt, p->size, p->wrap,
+                                     ctx->stream, &ctx->launches);
         else
-            e = launch_integrate_aos(ctx->bodies, part, js, n, p->dt, p->size, p->wrap, ctx->stream, &ctx->launches);
+            e = launch_integrate_aos(ctx->bodies, part, js, n, ctx->pending_G, p->dt, p->size, p->wrap, ctx->stream,
+                                     &ctx->launches);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "integrate launch");
         return NBODY_OK;
@@ -909,7 +913,7 @@ int nbody_cuda_dev_accel_soa(nbody_cuda* ctx, const void* pos_mass, const void* 
     const DirectPlan plan = plan_direct(n, p->law, false, ctx->force_variant);
     ctx->last_plan = plan;
     if (plan.jsplit > 1)
-        if (const int st = ensure_scratch(ctx, static_cast<size_t>(plan.jsplit) * n * sizeof(float4)))
+        if (const int st = ensure_scratch(ctx, direct_scratch_bytes(plan, n)))
             return st;
     const cudaError_t e = launch_direct(plan, static_cast<const float4*>(pos_mass), static_cast<const float4*>(vel_radius),
                                         static_cast<float4*>(acc), nullptr, static_cast<float4*>(ctx->scratch),
@@ -936,7 +940,7 @@ int nbody_cuda_dev_accel_aos(nbody_cuda* ctx, void* bodies, const size_t n, cons
     const DirectPlan plan = plan_direct(n, p->law, true, ctx->force_variant);
     ctx->last_plan = plan;
     if (plan.jsplit > 1)
-        if (const int st = ensure_scratch(ctx, static_cast<size_t>(plan.jsplit) * n * sizeof(float4)))
+        if (const int st = ensure_scratch(ctx, direct_scratch_bytes(plan, n)))
             return st;
     const cudaError_t e = launch_direct(plan, static_cast<const float4*>(bodies), nullptr, nullptr,
                                         static_cast<float*>(bodies), static_cast<float4*>(ctx->scratch),
@@ -961,7 +965,8 @@ int nbody_cuda_dev_integrate_soa(nbody_cuda* ctx, void* pos_mass, void* vel_radi
         return fail(ctx, NBODY_ERR_INVALID, "body count too large");
     const cudaError_t e = launch_integrate_soa(static_cast<float4*>(pos_mass), static_cast<float4*>(vel_radius),
                                                const_cast<float4*>(static_cast<const float4*>(acc)), nullptr, 0,
-                                               static_cast<int>(n), p->dt, p->size, p->wrap, ctx->stream, &ctx->launches);
+                                               static_cast<int>(n), p->G, p->dt, p->size, p->wrap, ctx->stream,
+                                               &ctx->launches);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "integrate launch");
     return NBODY_OK;

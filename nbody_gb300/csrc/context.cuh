@@ -41,6 +41,7 @@ struct nbody_cuda
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
     int pending_partials = 0;   // >1: scratch holds this many accelerate partials
+    float pending_G = 1.f;      // the G those partials are to be scaled by
 
     // Pinned host staging for pageable transfers.
     void* pinned = nullptr;

@@ -19,6 +19,13 @@
 //   - the source range can be split into `jsplit` chunks (blockIdx.y) so that the grid
 //     fills the 152 SMs evenly; chunk partials go to a scratch array and are summed in
 //     a fixed order (deterministic) by reduce_partials or the fused integrate.
+//   - summation: each 256-source tile is summed in FP32 from zero, and the tile sums are
+//     folded into an (S, C) pair per component by an error-free TwoSum, so S + C is the
+//     sum of the tile sums to about 2^-44 of their magnitude. A chunk leaves (S, C); the
+//     result is G * float(sum over chunks of S + C, in FP64). The tiles are the same 256
+//     sources for every kernel shape and split, so the result does not depend on the
+//     launch shape (up to a rounding tie of the last fold), and it is more accurate than
+//     one FP32 running sum over all N sources.
 #include <algorithm>
 #include <cstdio>
 
@@ -91,6 +98,16 @@ namespace nbg
         az = fma2(dz, s, az);
     }
 
+    // Fold one tile's FP32 sums t (two targets) into the thread's (S, C) pair, kept at
+    // sc[0] and sc[3 * stride] in shared memory: S + t = s + e exactly, S = s, C = C + e.
+    __device__ __forceinline__ void fold_tile(float2* sc, const int stride, const float2 t)
+    {
+        float2 s, e;
+        two_sum2(sc[0], t, s, e);
+        sc[0] = s;
+        sc[3 * stride] = add2(sc[3 * stride], e);
+    }
+
     // Source records: SoA streams one float4 {x,y,z,m} per body; AoS streams the whole
     // 48-byte Body (3 float4: {pos, radius}, {vel, mass}, {acc, pad}).
     template <bool AOS>
@@ -116,6 +133,12 @@ namespace nbg
         __shared__ __align__(128) float4 tile[STAGES][TILE * REC];
         __shared__ __align__(16) float4 pairs[DUP ? 2 * TILE : 1];
         __shared__ __align__(8) uint64_t bar[STAGES];
+        // Each thread's fold of its tile sums (dynamic shared memory, fold_bytes(T, BLOCK)):
+        // row 6p + c holds S of component c (x, y, z) of pair p, row 6p + 3 + c its
+        // compensation C; one column per thread, so a warp's accesses are conflict-free.
+        // Shared memory rather than registers: the 4 x 256 shape runs three CTAs per SM
+        // only within 85 registers.
+        extern __shared__ __align__(16) float2 fold[];
 
         const int tid = threadIdx.x;
         const int base = blockIdx.x * (BLOCK * T);
@@ -169,6 +192,9 @@ namespace nbg
             nz[p] = make_float2(q[0][2], q[1][2]);
             lim[p] = make_float2(q[0][3], q[1][3]);
             ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int r = 0; r < 6; ++r)
+                fold[(6 * p + r) * BLOCK + tid] = make_float2(0.f, 0.f);
         }
 
         int failed_at = -1;
@@ -225,6 +251,15 @@ namespace nbg
                         interact2<LAW, PACKED>(sx, sy, sz, sm, nx[p], ny[p], nz[p], lim[p], ax[p], ay[p], az[p]);
                 }
             }
+            // fold this tile's sums into (S, C) and start the next tile from zero
+#pragma unroll
+            for (int p = 0; p < P; ++p)
+            {
+                fold_tile(&fold[(6 * p) * BLOCK + tid], BLOCK, ax[p]);
+                fold_tile(&fold[(6 * p + 1) * BLOCK + tid], BLOCK, ay[p]);
+                fold_tile(&fold[(6 * p + 2) * BLOCK + tid], BLOCK, az[p]);
+                ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
+            }
             __syncthreads();
             if (tid == 0 && t + STAGES < ntiles)
                 issue(stage, t + STAGES);
@@ -243,18 +278,32 @@ namespace nbg
 #pragma unroll
         for (int p = 0; p < P; ++p)
         {
+            float2 S[3], Cc[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+            {
+                S[c] = fold[(6 * p + c) * BLOCK + tid];
+                Cc[c] = fold[(6 * p + 3 + c) * BLOCK + tid];
+            }
 #pragma unroll
             for (int h = 0; h < 2; ++h)
             {
                 const int i = base + tid + (2 * p + h) * BLOCK;
                 if (i >= n)
                     continue;
-                const float a0 = G * (h ? ax[p].y : ax[p].x);
-                const float a1 = G * (h ? ay[p].y : ay[p].x);
-                const float a2 = G * (h ? az[p].y : az[p].x);
+                const float4 s4 = make_float4(h ? S[0].y : S[0].x, h ? S[1].y : S[1].x, h ? S[2].y : S[2].x, 0.f);
+                const float4 c4 = make_float4(h ? Cc[0].y : Cc[0].x, h ? Cc[1].y : Cc[1].x, h ? Cc[2].y : Cc[2].x, 0.f);
                 if (partial)
-                    out[static_cast<size_t>(blockIdx.y) * n + i] = make_float4(a0, a1, a2, 0.f);
-                else if (AOS)
+                {
+                    // the chunk's unscaled (S, C); reduce_partials or the fused integrate sums
+                    // them over chunks in FP64 and applies G once
+                    out[(2 * static_cast<size_t>(blockIdx.y)) * n + i] = s4;
+                    out[(2 * static_cast<size_t>(blockIdx.y) + 1) * n + i] = c4;
+                    continue;
+                }
+                const float3 a = combine_partials(&s4, &c4, 1, 0, 0, G);
+                const float a0 = a.x, a1 = a.y, a2 = a.z;
+                if (AOS)
                 {
                     float* b = body_out + static_cast<size_t>(i) * 12 + 8;
                     b[0] = a0;
@@ -269,20 +318,13 @@ namespace nbg
 
     // Sum jsplit chunk partials in chunk order into acc (SoA float4) or Body::acc (AoS).
     __global__ void reduce_partials_kernel(const float4* __restrict__ part, const int jsplit,
-                                           const int n, float4* __restrict__ acc,
+                                           const int n, const float G, float4* __restrict__ acc,
                                            float* __restrict__ body_out)
     {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
         if (i >= n)
             return;
-        float4 a = part[i];
-        for (int s = 1; s < jsplit; ++s)
-        {
-            const float4 b = part[static_cast<size_t>(s) * n + i];
-            a.x += b.x;
-            a.y += b.y;
-            a.z += b.z;
-        }
+        const float3 a = combine_partials(part, part + n, jsplit, n, i, G);
         if (body_out)
         {
             float* b = body_out + static_cast<size_t>(i) * 12 + 8;
@@ -310,7 +352,19 @@ namespace nbg
             int T, block;
             bool packed, dup;
             KernelFn fn[2][2];  // [law][aos]
+            int fold_bytes;     // dynamic shared memory: the (S, C) fold, 6 float2 per target pair
         };
+
+        // Dynamic shared memory of a shape's fold array (6 float2 rows per target pair and
+        // one column per thread).
+        constexpr int fold_bytes_of(const int T, const int block) { return 6 * (T / 2) * block * 8; }
+
+        // Let fn take `bytes` of dynamic shared memory (beyond the 48 KB default where its
+        // static tiles and the fold need it). Cheap, and legal while a stream is captured.
+        void allow_dynamic_smem(const KernelFn fn, const int bytes)
+        {
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        }
 
         constexpr int kPlanned = 3;
 
@@ -326,6 +380,7 @@ namespace nbg
             v.fn[0][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_CUTOFF, true, PACKED, DUP>;
             v.fn[1][0] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, false, PACKED, DUP>;
             v.fn[1][1] = direct_fp32_kernel<T, B, kTile, kStages, NBODY_LAW_SOFTENED, true, PACKED, DUP>;
+            v.fold_bytes = fold_bytes_of(T, B);
             return v;
         }
 
@@ -360,11 +415,15 @@ namespace nbg
             return sms;
         }
 
-        int occupancy(KernelFn fn, const int block)
+        int occupancy(KernelFn fn, const int block, const int dyn_bytes)
         {
             int blocks = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block, 0) != cudaSuccess)
+            allow_dynamic_smem(fn, dyn_bytes);
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block, dyn_bytes) != cudaSuccess)
+            {
+                cudaGetLastError();
                 return 1;
+            }
             return blocks > 0 ? blocks : 1;
         }
     }
@@ -389,7 +448,8 @@ namespace nbg
                 const size_t per = static_cast<size_t>(vs[k].T) * vs[k].block;
                 const size_t tb = (n + per - 1) / per;
                 const size_t max_js = std::max<size_t>(1, n / (kTile * 4));
-                const size_t slots = static_cast<size_t>(occupancy(vs[k].fn[li][ai], vs[k].block)) * sms;
+                const size_t slots =
+                    static_cast<size_t>(occupancy(vs[k].fn[li][ai], vs[k].block, vs[k].fold_bytes)) * sms;
                 if (tb * max_js >= slots)
                 {
                     chosen = k;
@@ -402,7 +462,7 @@ namespace nbg
         const Variant& v = vs[chosen];
         const size_t per = static_cast<size_t>(v.T) * v.block;
         const size_t tb = std::max<size_t>(1, (n + per - 1) / per);
-        const size_t slots = static_cast<size_t>(occupancy(v.fn[li][ai], v.block)) * sms;
+        const size_t slots = static_cast<size_t>(occupancy(v.fn[li][ai], v.block, v.fold_bytes)) * sms;
         // Split the sources so tb*js CTAs pack into whole waves: minimise the padded
         // work ceil(tb*js/slots)*slots/(tb*js) per unit, preferring fewer chunks. Chunks may
         // be a single tile: at small n the target blocks alone would leave most SMs idle
@@ -453,13 +513,14 @@ namespace nbg
         const KernelFn fn = v.fn[plan.law == NBODY_LAW_SOFTENED ? 1 : 0][plan.aos ? 1 : 0];
         const dim3 grid(plan.grid_x, plan.jsplit);
         float4* out = plan.jsplit > 1 ? scratch : acc;
-        fn<<<grid, v.block, 0, stream>>>(src, vel_radius, out, plan.aos ? body_out : nullptr, n,
-                                         plan.chunk, G, eps2, err);
+        allow_dynamic_smem(fn, v.fold_bytes);
+        fn<<<grid, v.block, v.fold_bytes, stream>>>(src, vel_radius, out, plan.aos ? body_out : nullptr, n,
+                                                    plan.chunk, G, eps2, err);
         ++*launches;
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess || plan.jsplit <= 1 || !reduce)
             return e;
-        return launch_reduce(scratch, plan.jsplit, n, acc, plan.aos ? body_out : nullptr, stream, launches);
+        return launch_reduce(scratch, plan.jsplit, n, G, acc, plan.aos ? body_out : nullptr, stream, launches);
     }
 
     int direct_variant_count()
@@ -478,10 +539,10 @@ namespace nbg
         *packed = vs[i].dup ? 2 : (vs[i].packed ? 1 : 0);
     }
 
-    cudaError_t launch_reduce(const float4* scratch, const int jsplit, const int n, float4* acc,
+    cudaError_t launch_reduce(const float4* scratch, const int jsplit, const int n, const float G, float4* acc,
                               float* body_out, cudaStream_t stream, uint64_t* launches)
     {
-        reduce_partials_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(scratch, jsplit, n, acc, body_out);
+        reduce_partials_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(scratch, jsplit, n, G, acc, body_out);
         ++*launches;
         return cudaGetLastError();
     }

@@ -21,6 +21,33 @@ namespace nbg
         bool aos;
     };
 
+    // Bytes of j-split scratch one accelerate needs: per chunk and body, the chunk's FP32 sum
+    // S and its compensation C (two float4). None without a split.
+    inline size_t direct_scratch_bytes(const DirectPlan& plan, const size_t n)
+    {
+        return plan.jsplit > 1 ? 2 * static_cast<size_t>(plan.jsplit) * n * 16 : 0;
+    }
+
+    // The accelerations from the chunk partials of the FP32 direct sum: chunk c of body i
+    // holds its (S, C) at S[2 c n + i] and C[2 c n + i] (C = S + n in the scratch layout).
+    // The exact sums S + C are added over the chunks in chunk order in FP64, rounded to
+    // FP32 and scaled by G: the same formula for one chunk or many, so the result does not
+    // depend on how the sources were split.
+    __device__ __forceinline__ float3 combine_partials(const float4* __restrict__ S, const float4* __restrict__ C,
+                                                       const int js, const int n, const int i, const float G)
+    {
+        double x = 0.0, y = 0.0, z = 0.0;
+        for (int c = 0; c < js; ++c)
+        {
+            const size_t k = 2 * static_cast<size_t>(c) * n + i;
+            const float4 s = S[k], e = C[k];
+            x += static_cast<double>(s.x) + static_cast<double>(e.x);
+            y += static_cast<double>(s.y) + static_cast<double>(e.y);
+            z += static_cast<double>(s.z) + static_cast<double>(e.z);
+        }
+        return make_float3(G * static_cast<float>(x), G * static_cast<float>(y), G * static_cast<float>(z));
+    }
+
     // Pick a launch shape for n bodies. force_variant >= 0 pins the (T, block) entry.
     DirectPlan plan_direct(size_t n, int law, bool aos, int force_variant = -1);
 
@@ -30,23 +57,23 @@ namespace nbg
 
     // Queue the accelerate. src is pos_mass (SoA) or the Body array viewed as float4
     // (AoS). Results: acc (SoA) or Body::acc in body_out (AoS). scratch must hold
-    // plan.jsplit * n float4 when plan.jsplit > 1; with reduce == false the partials are
-    // left there for the fused integrate to sum.
+    // direct_scratch_bytes(plan, n); with reduce == false the partials are left there for
+    // the fused integrate to sum.
     cudaError_t launch_direct(const DirectPlan& plan, const float4* src, const float4* vel_radius,
                               float4* acc, float* body_out, float4* scratch, int n, float G,
                               float eps2, unsigned* err, cudaStream_t stream, uint64_t* launches,
                               bool reduce = true);
 
-    cudaError_t launch_reduce(const float4* scratch, int jsplit, int n, float4* acc,
+    cudaError_t launch_reduce(const float4* scratch, int jsplit, int n, float G, float4* acc,
                               float* body_out, cudaStream_t stream, uint64_t* launches);
 
-    // Semi-implicit Euler (integrate.cu). When part != nullptr the accelerations are the
-    // fixed-order sum of jsplit partials, also written to acc / Body::acc.
+    // Semi-implicit Euler (integrate.cu). When part != nullptr the accelerations are
+    // combine_partials over its jsplit chunks (with G), also written to acc / Body::acc.
     cudaError_t launch_integrate_soa(float4* pos_mass, float4* vel_radius, float4* acc,
-                                     const float4* part, int jsplit, int n, float dt, float size,
-                                     int wrap, cudaStream_t stream, uint64_t* launches);
+                                     const float4* part, int jsplit, int n, float G, float dt,
+                                     float size, int wrap, cudaStream_t stream, uint64_t* launches);
     cudaError_t launch_integrate_aos(float* bodies, const float4* part, int jsplit, int n,
-                                     float dt, float size, int wrap, cudaStream_t stream,
+                                     float G, float dt, float size, int wrap, cudaStream_t stream,
                                      uint64_t* launches);
 
     // Body (48 B) <-> split streams (integrate.cu).

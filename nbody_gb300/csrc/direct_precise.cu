@@ -749,7 +749,8 @@ namespace nbg
         {
             // an FP32 accelerate left partials for the fused FP32 integrate: sum them first
             const cudaError_t e = launch_reduce(static_cast<const float4*>(ctx->scratch), ctx->pending_partials,
-                                                static_cast<int>(ctx->count), ctx->layout == NBODY_LAYOUT_SOA ? ctx->acc : nullptr,
+                                                static_cast<int>(ctx->count), ctx->pending_G,
+                                                ctx->layout == NBODY_LAYOUT_SOA ? ctx->acc : nullptr,
                                                 ctx->layout == NBODY_LAYOUT_AOS ? ctx->bodies : nullptr, ctx->stream,
                                                 &ctx->launches);
             ctx->pending_partials = 0;

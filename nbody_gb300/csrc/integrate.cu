@@ -27,23 +27,9 @@ namespace nbg
         x = __fadd_rn(x, __fmul_rn(v, dt));
     }
 
-    __device__ __forceinline__ float3 sum_partials(const float4* __restrict__ part, const int js,
-                                                   const int n, const int i)
-    {
-        float4 a = part[i];
-        for (int s = 1; s < js; ++s)
-        {
-            const float4 b = part[static_cast<size_t>(s) * n + i];
-            a.x += b.x;
-            a.y += b.y;
-            a.z += b.z;
-        }
-        return make_float3(a.x, a.y, a.z);
-    }
-
     __global__ void integrate_soa_kernel(float4* __restrict__ pm, float4* __restrict__ vr,
                                          float4* __restrict__ acc, const float4* __restrict__ part,
-                                         const int js, const int n, const float dt,
+                                         const int js, const int n, const float G, const float dt,
                                          const float size, const int wrap)
     {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -54,7 +40,7 @@ namespace nbg
         float3 a;
         if (part)
         {
-            a = sum_partials(part, js, n, i);
+            a = combine_partials(part, part + n, js, n, i, G);
             acc[i] = make_float4(a.x, a.y, a.z, 0.f);
         }
         else
@@ -76,7 +62,7 @@ namespace nbg
     }
 
     __global__ void integrate_aos_kernel(float* __restrict__ bodies, const float4* __restrict__ part,
-                                         const int js, const int n, const float dt,
+                                         const int js, const int n, const float G, const float dt,
                                          const float size, const int wrap)
     {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -88,7 +74,7 @@ namespace nbg
         float4 a = b[2];    // acc, pad
         if (part)
         {
-            const float3 s = sum_partials(part, js, n, i);
+            const float3 s = combine_partials(part, part + n, js, n, i, G);
             a.x = s.x;
             a.y = s.y;
             a.z = s.z;
@@ -144,23 +130,24 @@ namespace nbg
     }
 
     cudaError_t launch_integrate_soa(float4* pm, float4* vr, float4* acc, const float4* part,
-                                     const int js, const int n, const float dt, const float size,
+                                     const int js, const int n, const float G, const float dt, const float size,
                                      const int wrap, cudaStream_t stream, uint64_t* launches)
     {
         if (n <= 0)
             return cudaSuccess;
-        integrate_soa_kernel<<<ceil_div(n, kBlock), kBlock, 0, stream>>>(pm, vr, acc, part, js, n, dt, size, wrap);
+        integrate_soa_kernel<<<ceil_div(n, kBlock), kBlock, 0, stream>>>(pm, vr, acc, part, js, n, G, dt, size,
+                                                                          wrap);
         ++*launches;
         return cudaGetLastError();
     }
 
     cudaError_t launch_integrate_aos(float* bodies, const float4* part, const int js, const int n,
-                                     const float dt, const float size, const int wrap,
+                                     const float G, const float dt, const float size, const int wrap,
                                      cudaStream_t stream, uint64_t* launches)
     {
         if (n <= 0)
             return cudaSuccess;
-        integrate_aos_kernel<<<ceil_div(n, kBlock), kBlock, 0, stream>>>(bodies, part, js, n, dt, size, wrap);
+        integrate_aos_kernel<<<ceil_div(n, kBlock), kBlock, 0, stream>>>(bodies, part, js, n, G, dt, size, wrap);
         ++*launches;
         return cudaGetLastError();
     }

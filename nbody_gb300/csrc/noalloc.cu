@@ -150,11 +150,12 @@ extern "C" int nbody_cuda_dev_accel_soa_noalloc(const void* pos_mass, const void
     if (device_scratch(&s) != cudaSuccess)
         return NBODY_ERR_CUDA;
 
-    // The usual launch shape, with the source split capped so its partials fit.
+    // The usual launch shape, with the source split capped so its partials fit: a chunk
+    // leaves two float4 per body (its sum and the sum's compensation).
     DirectPlan plan = plan_direct(n, p->law, false);
-    if (static_cast<size_t>(plan.jsplit) * n > kNoAllocPartials)
+    if (direct_scratch_bytes(plan, n) > kNoAllocPartials * sizeof(float4))
     {
-        const size_t js = std::max<size_t>(1, kNoAllocPartials / n);
+        const size_t js = std::max<size_t>(1, kNoAllocPartials / (2 * n));
         size_t chunk = (n + js - 1) / js;
         chunk = (chunk + plan.tile - 1) / plan.tile * plan.tile;
         plan.chunk = static_cast<int>(chunk);

@@ -22,6 +22,7 @@ LAYOUT_SOA, LAYOUT_AOS = 0, 1
 READ_POSITIONS, READ_VELOCITIES, READ_ACCELERATIONS, READ_ALL = 1, 2, 4, 7
 QUERY_ALL, QUERY_FIRST_BODY = 0, 1
 TRANSFER_AUTO, TRANSFER_STAGED, TRANSFER_MAPPED, TRANSFER_DIRECT = 0, 1, 2, 3
+WALK_TARGET, WALK_GROUP = 0, 1
 
 # bh::Node (include/nbody/bhtree.h of the reference): bounds centre, size, com, mass, links
 NODE_DTYPE = np.dtype([("center", "<f4", 3), ("size", "<f4"), ("com", "<f4", 3), ("mass", "<f4"),
@@ -51,7 +52,7 @@ class StepParams(C.Structure):
     """nbody_step_params."""
     _fields_ = [("dt", C.c_float), ("theta", C.c_float), ("G", C.c_float), ("eps2", C.c_float),
                 ("size", C.c_float), ("wrap", C.c_int32), ("mode", C.c_int32), ("law", C.c_int32),
-                ("precision", C.c_int32), ("tree_box", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("precision", C.c_int32), ("tree_box", C.c_int32), ("walk", C.c_int32), ("reserved", C.c_int32)]
 
 
 class DiskArgs(C.Structure):
@@ -80,8 +81,8 @@ def cube_args(center=(0.0, 0.0, 0.0), size=500.0, vel=(0.0, 0.0, 0.0), star_mass
 
 
 def params(dt=0.0, theta=0.5, G=1.0, eps2=0.0, size=10000.0, wrap=False, mode=MODE_N2,
-           law=LAW_CUTOFF, precision=PREC_FP32, tree_box=0) -> StepParams:
-    return StepParams(dt, theta, G, eps2, size, int(bool(wrap)), mode, law, precision, tree_box)
+           law=LAW_CUTOFF, precision=PREC_FP32, tree_box=0, walk=WALK_TARGET) -> StepParams:
+    return StepParams(dt, theta, G, eps2, size, int(bool(wrap)), mode, law, precision, tree_box, walk, 0)
 
 
 class NbodyError(RuntimeError):

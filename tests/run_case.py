@@ -24,6 +24,7 @@ def main(argv=None) -> int:
     ap.add_argument("--n", type=int, default=1 << 18)
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--walk", type=int, default=0, help="Barnes-Hut walk: 0 per target, 1 per group")
     ap.add_argument("--variant", type=int, default=-1,
                     help="pin a direct-sum kernel shape (batched: the batched configuration)")
     a = ap.parse_args(argv)
@@ -46,7 +47,7 @@ def main(argv=None) -> int:
         n_disk = int(round(a.n * 12_000_000 / 16_777_216))
         bodies = scenes.disk_halo(n_disk=n_disk, n_halo=a.n - n_disk)
         p = native.params(mode=native.MODE_NLOGN, theta=a.theta, law=native.LAW_SOFTENED, eps2=0.005 ** 2,
-                          dt=2.5e-4, size=0.0, tree_box=1, precision=native.PREC_COMPENSATED)
+                          dt=2.5e-4, size=0.0, tree_box=1, precision=native.PREC_COMPENSATED, walk=a.walk)
         with native.Context() as ctx:
             ctx.upload_bodies(bodies)
             ctx.update(p, a.steps)
