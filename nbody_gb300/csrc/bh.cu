@@ -1333,6 +1333,12 @@ namespace nbg
 #pragma unroll
             for (int g = 0; g < NSG; ++g)
                 all |= cnt[g] > 0 ? (1u << g) : 0u;
+            // the sub-groups present among each target pair's targets, over the warp: a
+            // partial entry none of them takes skips that pair (a uniform branch)
+            unsigned pair_groups[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+                pair_groups[q] = __reduce_or_sync(0xffffffffu, bit[2 * q] | bit[2 * q + 1]);
             __syncwarp();       // the previous group's readers of box/cnt are done
             if (lane < 2 * NSG)
             {
@@ -1373,8 +1379,9 @@ namespace nbg
                     const unsigned m = pmask[e];
 #pragma unroll
                     for (int q = 0; q < Q; ++q)
-                        apply_list2<LAW, true>(npx[q], npy[q], npz[q], lim[q], s, (m & bit[2 * q]) != 0u,
-                                               (m & bit[2 * q + 1]) != 0u, ax[q], ay[q], az[q]);
+                        if (m & pair_groups[q])
+                            apply_list2<LAW, true>(npx[q], npy[q], npz[q], lim[q], s, (m & bit[2 * q]) != 0u,
+                                                   (m & bit[2 * q + 1]) != 0u, ax[q], ay[q], az[q]);
                     inter += static_cast<unsigned long long>(cnt_of[m]);
                 }
                 fn_ = 0;

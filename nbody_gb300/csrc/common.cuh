@@ -131,6 +131,16 @@ namespace nbg
         return __fadd2_rn(a, make_float2(-b.x, -b.y));
     }
 
+    // Error-free transformation of a sum (Knuth's TwoSum): s = fl(a + b) and
+    // e = (a + b) - s exactly, for any a and b. Six additions, none reassociated (the
+    // intrinsics are never contracted or reordered).
+    __device__ __forceinline__ void two_sum(const float a, const float b, float& s, float& e)
+    {
+        s = __fadd_rn(a, b);
+        const float bb = __fsub_rn(s, a);
+        e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    }
+
     // Error-free transformation of a sum (Knuth's TwoSum), per half: s = fl(a + b) and
     // e = (a + b) - s exactly, for any a and b (no ordering of magnitudes needed). Six
     // additions, none of which may be reassociated; packed adds are never contracted.

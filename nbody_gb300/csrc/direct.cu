@@ -22,7 +22,8 @@
 //   - summation: each 256-source tile is summed in FP32 from zero, and the tile sums are
 //     folded into an (S, C) pair per component by an error-free TwoSum, so S + C is the
 //     sum of the tile sums to about 2^-44 of their magnitude. A chunk leaves (S, C); the
-//     result is G * float(sum over chunks of S + C, in FP64). The tiles are the same 256
+//     result is G * float(sum over chunks of S + C, as a double-float sum; direct.cuh
+//     combine_partials). The tiles are the same 256
 //     sources for every kernel shape and split, so the result does not depend on the
 //     launch shape (up to a rounding tie of the last fold), and it is more accurate than
 //     one FP32 running sum over all N sources.

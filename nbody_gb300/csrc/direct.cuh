@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "common.cuh"
+
 namespace nbg
 {
     // Launch shape of one direct-sum accelerate.
@@ -30,22 +32,31 @@ namespace nbg
 
     // The accelerations from the chunk partials of the FP32 direct sum: chunk c of body i
     // holds its (S, C) at S[2 c n + i] and C[2 c n + i] (C = S + n in the scratch layout).
-    // The exact sums S + C are added over the chunks in chunk order in FP64, rounded to
-    // FP32 and scaled by G: the same formula for one chunk or many, so the result does not
-    // depend on how the sources were split.
+    // The pairs are added over the chunks in chunk order as a double-float sum (TwoSum into
+    // a running (s, e), the compensations added to e), then s + e is rounded to FP32 and
+    // scaled by G: the same formula for one chunk or many, so the result does not depend on
+    // how the sources were split. FP32 only: GB300's FP64 pipe runs at 1/64 of the FP32
+    // rate, and a small system's few bodies would put that work on a few SMs.
     __device__ __forceinline__ float3 combine_partials(const float4* __restrict__ S, const float4* __restrict__ C,
                                                        const int js, const int n, const int i, const float G)
     {
-        double x = 0.0, y = 0.0, z = 0.0;
+        float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
         for (int c = 0; c < js; ++c)
         {
             const size_t k = 2 * static_cast<size_t>(c) * n + i;
             const float4 s = S[k], e = C[k];
-            x += static_cast<double>(s.x) + static_cast<double>(e.x);
-            y += static_cast<double>(s.y) + static_cast<double>(e.y);
-            z += static_cast<double>(s.z) + static_cast<double>(e.z);
+            float t, r;
+            two_sum(sx, s.x, t, r);
+            sx = t;
+            ex = __fadd_rn(ex, __fadd_rn(r, e.x));
+            two_sum(sy, s.y, t, r);
+            sy = t;
+            ey = __fadd_rn(ey, __fadd_rn(r, e.y));
+            two_sum(sz, s.z, t, r);
+            sz = t;
+            ez = __fadd_rn(ez, __fadd_rn(r, e.z));
         }
-        return make_float3(G * static_cast<float>(x), G * static_cast<float>(y), G * static_cast<float>(z));
+        return make_float3(G * __fadd_rn(sx, ex), G * __fadd_rn(sy, ey), G * __fadd_rn(sz, ez));
     }
 
     // Pick a launch shape for n bodies. force_variant >= 0 pins the (T, block) entry.
