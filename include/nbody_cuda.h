@@ -396,6 +396,16 @@ int nbody_cuda_batch_set_config(nbody_cuda* ctx, int index);
  * SOFTENED, else unsoftened), momentum xyz. O(sum of N_s^2) FP64 work. Synchronous. */
 int nbody_cuda_system_energy(nbody_cuda* ctx, const nbody_step_params* p, double* out, size_t nsys);
 
+/* Energy and momentum of all bodies at the direct sum's rate, for runs too large for the
+ * FP64 diagnostics above: out[0] = kinetic energy, out[1] = potential energy (softened
+ * with eps2 under the SOFTENED law, else unsoftened), out[2..4] = momentum. Pair terms
+ * are FP32 (rsqrt on the SFU), summed in FP32 over 256-source tiles whose sums are folded
+ * exactly, per body in FP64, over each pair once; every total is an FP64 sum in a fixed
+ * order, so the result is deterministic and the potential is within about 1e-7 of the FP64
+ * one. Pairs at zero separation are left out. O(N^2 / 2) FP32 work. Synchronous. No
+ * reference counterpart. */
+int nbody_cuda_energy(nbody_cuda* ctx, const nbody_step_params* p, double out[5]);
+
 /* `steps` x update, with one step captured as a CUDA graph and replayed: the first step
  * runs eagerly (it sets up every buffer), the step is captured once per parameter set,
  * body count, stream and buffer generation, and replayed for the remaining steps. Results

@@ -802,6 +802,19 @@ int nbody_cuda_system_energy(nbody_cuda* ctx, const nbody_step_params* p, double
     return batch_energy(ctx, &q, out);
 }
 
+int nbody_cuda_energy(nbody_cuda* ctx, const nbody_step_params* p, double out[5])
+{
+    if (!ctx || !out)
+        return NBODY_ERR_INVALID;
+    if (const int st = check_params(ctx, p))
+        return st;
+    if (ctx->capturing)
+        return fail(ctx, NBODY_ERR_UNSUPPORTED, "energy diagnostics are synchronous");
+    if (const int st = energy_all(ctx, p, out))
+        return st;
+    return check_device_error(ctx);
+}
+
 int nbody_cuda_update_graph(nbody_cuda* ctx, const nbody_step_params* p, const int steps)
 {
     if (!ctx)

@@ -183,4 +183,7 @@ namespace nbg
     // bh.cu
     int bh_accelerate(nbody_cuda* ctx, const nbody_step_params* p);
     void release_bh(nbody_cuda* ctx);
+
+    // energy.cu: kinetic, potential energy and momentum of all bodies (nbody_cuda_energy)
+    int energy_all(nbody_cuda* ctx, const nbody_step_params* p, double out[5]);
 }

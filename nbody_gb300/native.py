@@ -45,6 +45,7 @@ EXPORTS = (
     "nbody_cuda_direct_variant", "nbody_cuda_set_direct_variant", "nbody_cuda_direct_autotune",
     "nbody_cuda_selftest_wait", "nbody_cuda_set_transfer", "nbody_cuda_transfer_info",
     "nbody_cuda_prefetch", "nbody_cuda_scene_disk", "nbody_cuda_scene_cube", "nbody_cuda_tree_query",
+    "nbody_cuda_energy",
 )
 
 
@@ -142,6 +143,7 @@ def lib() -> C.CDLL:
         "nbody_cuda_batch_config": ([vp, C.c_int] + [C.POINTER(C.c_int)] * 3, C.c_int),
         "nbody_cuda_batch_set_config": ([vp, C.c_int], C.c_int),
         "nbody_cuda_system_energy": ([vp, P, vp, sz], C.c_int),
+        "nbody_cuda_energy": ([vp, P, C.POINTER(C.c_double)], C.c_int),
         "nbody_cuda_update_graph": ([vp, P, C.c_int], C.c_int),
         "nbody_cuda_direct_variant_count": ([], C.c_int),
         "nbody_cuda_direct_variant": ([C.c_int] + [C.POINTER(C.c_int)] * 3, C.c_int),
@@ -353,6 +355,12 @@ class Context:
 
     def batch_set_config(self, index: int):
         self.check(lib().nbody_cuda_batch_set_config(self.h, index))
+
+    def energy(self, p: StepParams) -> dict:
+        """nbody_cuda_energy: kinetic and potential energy and momentum of all bodies."""
+        out = (C.c_double * 5)()
+        self.check(lib().nbody_cuda_energy(self.h, C.byref(p), out))
+        return {"kinetic": out[0], "potential": out[1], "momentum": np.array(out[2:5])}
 
     def system_energy(self, p: StepParams, nsys: int | None = None) -> np.ndarray:
         n = nsys or getattr(self, "nsys", 1) or 1

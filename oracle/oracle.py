@@ -32,75 +32,87 @@ LAW_CUTOFF = 0
 LAW_SOFTENED = 1
 
 _lib = None
+_timing = None
 _ref = None
+_ref_timing = None
 
 
 def _p(a, t):
     return a.ctypes.data_as(t) if a is not None else None
 
 
-def lib():
-    global _lib
+def lib(timing: bool = False):
+    """The oracle library; timing=True gives the same source built for speed (the CPU
+    baselines only: its last bits are not the checked ones)."""
+    global _lib, _timing
+    if timing:
+        if _timing is None:
+            _timing = _bind(C.CDLL(str(build_oracle.build_oracle_timing())))
+        return _timing
     if _lib is None:
-        path = build_oracle.build_oracle()
-        L = C.CDLL(str(path))
-        L.orc_gravity.argtypes = [_F, C.c_float, _F, C.c_float, C.c_float, _F]
-        L.orc_wrap.argtypes = [C.c_float, C.c_float]
-        L.orc_wrap.restype = C.c_float
-        L.orc_integrate.argtypes = [_F, _SZ, C.c_float, C.c_float, C.c_int]
-        L.orc_brute_force.argtypes = [_F, _SZ, C.c_float, C.c_int]
-        L.orc_brute_force_targets.argtypes = [_F, _SZ, C.c_float, _I64, _SZ, _F, C.c_int]
-        L.orc_barnes_hut.argtypes = [_F, _SZ, C.c_float, C.c_float, C.c_float, C.c_int, _U64]
-        L.orc_gravity_softened.argtypes = [_F, _F, C.c_float, C.c_float, C.c_float, _F]
-        L.orc_brute_force_targets_law.argtypes = [_F, _SZ, C.c_float, C.c_int, C.c_float, _I64, _SZ, _F, C.c_int]
-        L.orc_barnes_hut_law.argtypes = [_F, _SZ, C.c_float, C.c_float, C.c_float, C.c_int, C.c_float, C.c_int,
-                                         _U64]
-        L.orc_tree_accel_law.argtypes = [C.c_void_p, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, C.c_int, C.c_float,
-                                         _F, _U64, C.c_int]
-        L.orc_nodes_accel_law.argtypes = [C.c_void_p, _SZ, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, C.c_int,
-                                          C.c_float, _F, _U64, C.c_int]
-        L.orc_tree_new.argtypes = [C.c_float]
-        L.orc_tree_new.restype = C.c_void_p
-        L.orc_tree_free.argtypes = [C.c_void_p]
-        L.orc_tree_clear.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
-        L.orc_tree_insert.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
-        L.orc_tree_build.argtypes = [C.c_void_p, _F, _SZ, C.c_float]
-        L.orc_tree_build_box.argtypes = [C.c_void_p, _F, _SZ, C.c_float, C.c_float, C.c_float, C.c_float]
-        L.orc_tree_exact_moments.argtypes = [C.c_void_p, _F, _SZ]
-        L.orc_tree_exact_moments.restype = C.c_int
-        L.orc_tree_size.argtypes = [C.c_void_p]
-        L.orc_tree_size.restype = _SZ
-        L.orc_tree_nodes.argtypes = [C.c_void_p]
-        L.orc_tree_nodes.restype = C.c_void_p
-        L.orc_tree_accel.argtypes = [C.c_void_p, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, _F, _U64, C.c_int]
-        L.orc_nodes_accel.argtypes = [C.c_void_p, _SZ, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, _F, _U64, C.c_int]
-        L.orc_direct_f64.argtypes = [_F, _F, _SZ, C.c_double, C.c_double, C.c_int, _I64, _SZ, _D, _D, C.c_int]
-        L.orc_direct_f64_pos.argtypes = [_D, _D, _SZ, C.c_double, C.c_double, _I64, _SZ, _D, C.c_int]
-        L.orc_energy_f64.argtypes = [_D, _D, _D, _SZ, C.c_double, C.c_double, _D, _D, _D, C.c_int]
-        L.orc_morton63.argtypes = [_F, _SZ, _SZ, _D, C.c_double, _U64]
-        L.orc_sort_order.argtypes = [_U64, _SZ, _U32]
-        L.orc_default_threads.restype = C.c_int
-        L.orc_minstd_value.argtypes = [C.c_uint64]
-        L.orc_minstd_value.restype = C.c_uint32
-        L.orc_compute_radius.argtypes = [C.c_float, C.c_float]
-        L.orc_compute_radius.restype = C.c_float
-        L.orc_disk.argtypes = [_F, _SZ, _F]
-        L.orc_cube.argtypes = [_F, _SZ, _F]
-        L.orc_disk_positions.argtypes = [_F, _SZ, _F, _SZ, _SZ]
-        L.orc_tree_query.argtypes = [C.c_void_p, _SZ, _F, C.c_int, _U32, _SZ, C.POINTER(C.c_int)]
-        L.orc_tree_query.restype = _SZ
-        _lib = L
+        _lib = _bind(C.CDLL(str(build_oracle.build_oracle())))
     return _lib
 
 
-def ref_lib():
-    """The reference's own CPU solvers, or None where they could not be built."""
-    global _ref
-    if _ref is None:
-        path = build_oracle.REF_LIB
+def _bind(L):
+    """Argument and result types of every oracle entry point."""
+    L.orc_gravity.argtypes = [_F, C.c_float, _F, C.c_float, C.c_float, _F]
+    L.orc_wrap.argtypes = [C.c_float, C.c_float]
+    L.orc_wrap.restype = C.c_float
+    L.orc_integrate.argtypes = [_F, _SZ, C.c_float, C.c_float, C.c_int]
+    L.orc_brute_force.argtypes = [_F, _SZ, C.c_float, C.c_int]
+    L.orc_brute_force_targets.argtypes = [_F, _SZ, C.c_float, _I64, _SZ, _F, C.c_int]
+    L.orc_barnes_hut.argtypes = [_F, _SZ, C.c_float, C.c_float, C.c_float, C.c_int, _U64]
+    L.orc_gravity_softened.argtypes = [_F, _F, C.c_float, C.c_float, C.c_float, _F]
+    L.orc_brute_force_targets_law.argtypes = [_F, _SZ, C.c_float, C.c_int, C.c_float, _I64, _SZ, _F, C.c_int]
+    L.orc_barnes_hut_law.argtypes = [_F, _SZ, C.c_float, C.c_float, C.c_float, C.c_int, C.c_float, C.c_int,
+                                     _U64]
+    L.orc_tree_accel_law.argtypes = [C.c_void_p, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, C.c_int, C.c_float,
+                                     _F, _U64, C.c_int]
+    L.orc_nodes_accel_law.argtypes = [C.c_void_p, _SZ, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, C.c_int,
+                                      C.c_float, _F, _U64, C.c_int]
+    L.orc_tree_new.argtypes = [C.c_float]
+    L.orc_tree_new.restype = C.c_void_p
+    L.orc_tree_free.argtypes = [C.c_void_p]
+    L.orc_tree_clear.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
+    L.orc_tree_insert.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
+    L.orc_tree_build.argtypes = [C.c_void_p, _F, _SZ, C.c_float]
+    L.orc_tree_build_box.argtypes = [C.c_void_p, _F, _SZ, C.c_float, C.c_float, C.c_float, C.c_float]
+    L.orc_tree_exact_moments.argtypes = [C.c_void_p, _F, _SZ]
+    L.orc_tree_exact_moments.restype = C.c_int
+    L.orc_tree_size.argtypes = [C.c_void_p]
+    L.orc_tree_size.restype = _SZ
+    L.orc_tree_nodes.argtypes = [C.c_void_p]
+    L.orc_tree_nodes.restype = C.c_void_p
+    L.orc_tree_accel.argtypes = [C.c_void_p, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, _F, _U64, C.c_int]
+    L.orc_nodes_accel.argtypes = [C.c_void_p, _SZ, _F, _SZ, _I64, _SZ, C.c_float, C.c_float, _F, _U64, C.c_int]
+    L.orc_direct_f64.argtypes = [_F, _F, _SZ, C.c_double, C.c_double, C.c_int, _I64, _SZ, _D, _D, C.c_int]
+    L.orc_direct_f64_pos.argtypes = [_D, _D, _SZ, C.c_double, C.c_double, _I64, _SZ, _D, C.c_int]
+    L.orc_energy_f64.argtypes = [_D, _D, _D, _SZ, C.c_double, C.c_double, _D, _D, _D, C.c_int]
+    L.orc_morton63.argtypes = [_F, _SZ, _SZ, _D, C.c_double, _U64]
+    L.orc_sort_order.argtypes = [_U64, _SZ, _U32]
+    L.orc_default_threads.restype = C.c_int
+    L.orc_minstd_value.argtypes = [C.c_uint64]
+    L.orc_minstd_value.restype = C.c_uint32
+    L.orc_compute_radius.argtypes = [C.c_float, C.c_float]
+    L.orc_compute_radius.restype = C.c_float
+    L.orc_disk.argtypes = [_F, _SZ, _F]
+    L.orc_cube.argtypes = [_F, _SZ, _F]
+    L.orc_disk_positions.argtypes = [_F, _SZ, _F, _SZ, _SZ]
+    L.orc_tree_query.argtypes = [C.c_void_p, _SZ, _F, C.c_int, _U32, _SZ, C.POINTER(C.c_int)]
+    L.orc_tree_query.restype = _SZ
+    return L
+
+
+def ref_lib(timing: bool = False):
+    """The reference's own CPU solvers, or None where they could not be built; timing=True
+    gives them built with the timing flags."""
+    global _ref, _ref_timing
+    if (_ref_timing if timing else _ref) is None:
+        path = build_oracle.REF_TIMING_LIB if timing else build_oracle.REF_LIB
         if not path.exists():
             try:
-                path = build_oracle.build_ref()
+                path = build_oracle.build_ref(timing=timing)
             except RuntimeError:
                 path = None
         if path is None or not Path(path).exists():
@@ -123,8 +135,11 @@ def ref_lib():
         L.ref_tree_query.argtypes = [_F, _SZ, C.c_float, _F, C.c_int, _U32, _SZ]
         L.ref_tree_query.restype = _SZ
         L.ref_cube_args.argtypes = [_F, _SZ, _SZ, _SZ, _F]
-        _ref = L
-    return _ref
+        if timing:
+            _ref_timing = L
+        else:
+            _ref = L
+    return _ref_timing if timing else _ref
 
 
 def threads() -> int:
@@ -170,22 +185,24 @@ def gravity_softened(pos, src, src_mass, G, eps2):
     return out
 
 
-def brute_force_targets(bodies, G, targets, nthreads=0, law=LAW_CUTOFF, eps2=0.0):
+def brute_force_targets(bodies, G, targets, nthreads=0, law=LAW_CUTOFF, eps2=0.0, timing=False):
     """CpuBruteForceSolver::accelerate (cpu_brute_force.h:17-43) for the listed targets, with
-    the reference's cutoff law or the softened law (eps2)."""
+    the reference's cutoff law or the softened law (eps2); timing=True runs the speed build."""
     b = _bodies(bodies)
     t = np.ascontiguousarray(targets, np.int64)
     out = np.zeros((len(t), 3), np.float32)
-    lib().orc_brute_force_targets_law(_p(b, _F), len(b), G, law, eps2, _p(t, _I64), len(t), _p(out, _F), nthreads)
+    lib(timing).orc_brute_force_targets_law(_p(b, _F), len(b), G, law, eps2, _p(t, _I64), len(t), _p(out, _F),
+                                            nthreads)
     return out
 
 
-def barnes_hut(bodies, size, theta, G, nthreads=0, law=LAW_CUTOFF, eps2=0.0):
+def barnes_hut(bodies, size, theta, G, nthreads=0, law=LAW_CUTOFF, eps2=0.0, timing=False):
     """CpuBarnesHutSolver::accelerate restated; returns (bodies with acc, interactions).
-    law/eps2 choose the visitor's force law (the reference's cutoff law by default)."""
+    law/eps2 choose the visitor's force law (the reference's cutoff law by default);
+    timing=True runs the speed build."""
     b = _bodies(bodies).copy()
     inter = np.zeros(1, np.uint64)
-    lib().orc_barnes_hut_law(_p(b, _F), len(b), size, theta, G, law, eps2, nthreads, _p(inter, _U64))
+    lib(timing).orc_barnes_hut_law(_p(b, _F), len(b), size, theta, G, law, eps2, nthreads, _p(inter, _U64))
     return b, int(inter[0])
 
 
