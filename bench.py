@@ -20,29 +20,36 @@ Printed JSON line (rank 0):
                   form against FP64 on 65,536 sampled targets (the FP64 reference is the
                   GPU FP64 form, itself checked against the CPU oracle on 512 targets).
   barnes_hut_16m  N = 16,777,216 exponential disk + Hernquist halo, eps = 0.005,
-                  dt = 2.5e-4, FP32 tree forces + compensated integration, reference-
-                  convention theta 0.5 and 0.75: steps/s, interactions, tree cells, the
-                  device time of the build and of the traversal (nbody_cuda_bh_stage_ms),
-                  the build's compulsory bytes against the measured HBM copy bandwidth,
-                  and the traversal's interactions (20 flop each) against the FFMA peak.
+                  dt = 2.5e-4, FP32 tree forces + compensated integration, at reference-
+                  convention theta 0.5 and 0.75 and conventional theta 0.5 and 0.75
+                  (reference theta 2 and 4/3), each with both walks (per target, per
+                  group with interaction lists): steps/s, interactions, the device time of
+                  the build and of the traversal (nbody_cuda_bh_stage_ms), the build's
+                  compulsory bytes against the measured HBM copy bandwidth, the traversal's
+                  interactions (20 flop each) against the FFMA peak, and the median / p99
+                  relative error against the FP64 direct sum on 4096 sampled targets. Its
+                  "drift_100_steps" object runs config 5's 100 steps and reports the energy
+                  and momentum drift from nbody_cuda_energy at both ends.
                   Its "transfer" object times the host transfer paths (staged, mapped,
                   direct) for all 16.8M Body records against the copy engine's pinned
                   bandwidth, and one frame of update + state(). Its "cpu_reference_bh"
                   object times one full step of the restated CPU Barnes-Hut on the same
                   bodies on all host cores.
-  configs         configs 1 (N = 4096 Plummer, 100 steps) and 2 (2 x 131072 Plummer BH),
-                  each beside the reference's CPU solver on the same bodies and host cores
-                  (all 100 steps of config 1; one step of config 2).
+  configs         configs 1 (N = 4096 Plummer, 100 steps) and 2 (2 x 131072 Plummer BH,
+                  both theta conventions and walks, with FP64 errors on 4096 sampled
+                  targets), each beside the reference's CPU solver (restated, softened law)
+                  on the same bodies and host cores (all 100 steps of config 1; one step
+                  of config 2), and config 4 (512 batched systems).
   scene_generators util::disk and util::cube on the device at N = 16,777,216, against the
                   reference's serial generator on 1,048,576 bodies.
   ray_query       Tree::query over the exported tree of 1,048,576 bodies: picking rays
                   and full walks per second, against the walk on one host core.
-  cpu_baseline    the reference's CPU brute force (oracle/_ref, built from the reference's
-                  sources) where it loads, else the oracle's C restatement, on all host
-                  cores, timed on a bounded sample of targets against all N sources.
+  cpu_baseline    the reference's CPU brute force, restated in the oracle (speed build), with
+                  the GPU arm's softened law, on all host cores, timed on a bounded sample
+                  of targets against all N sources.
 
-``--impl reference`` times only the CPU implementation (same workload, metric and
-units) and prints its own line.
+``--impl reference`` times only that CPU implementation on the same workload, metric and
+units, a bounded sample of targets per step, and prints its own line.
 """
 from __future__ import annotations
 
@@ -139,61 +146,52 @@ class ClockSampler:
 
 # --- CPU baseline -------------------------------------------------------------------------
 
-def cpu_brute_force_rate(bodies: np.ndarray, seconds: float = 10.0):
-    """Pairs/s of the reference CPU brute force (or its restatement) on all host cores,
-    timed on a bounded sample of the workload."""
+def cpu_brute_force_rate(bodies: np.ndarray, seconds: float = 10.0, eps2: float = EPS * EPS):
+    """Pairs/s of the reference's CPU brute force (CpuBruteForceSolver::accelerate,
+    cpu_brute_force.h:17-43, restated in oracle/nbody_oracle.c) with the GPU arm's own
+    softened law, on all host cores, timed on a bounded sample of the workload: k sampled
+    targets against all n sources. The restatement is timed in its speed build (-O2, the
+    reference's fastest build); the reference's own sources do not exist on the GPU host."""
     from oracle import oracle as O
     n = len(bodies)
     threads = O.threads()
-    if O.ref_available():
-        # the reference solver sums over all of its bodies: time it on a k-body prefix
-        k = 2048
-        while True:
-            t0 = time.perf_counter()
-            O.ref_brute_force(bodies[:k], 1.0, nthreads=threads)
-            dt = time.perf_counter() - t0
-            if dt >= seconds / 4 or k >= n:
-                break
-            k = min(n, int(k * max(1.5, min(4.0, np.sqrt(seconds / max(dt, 1e-3))))))
-        return k * k / dt, threads, "reference", \
-            f"CpuBruteForceSolver::accelerate on the first {k} bodies (all {k}x{k} pairs), {dt:.1f} s"
     k = 64
     while True:
         tg = np.linspace(0, n - 1, k).astype(np.int64)
         t0 = time.perf_counter()
-        O.brute_force_targets(bodies, 1.0, tg, nthreads=threads)
+        O.brute_force_targets(bodies, 1.0, tg, nthreads=threads, law=O.LAW_SOFTENED, eps2=eps2, timing=True)
         dt = time.perf_counter() - t0
         if dt >= seconds / 4:
             break
         k = int(k * min(8.0, max(2.0, seconds / max(dt, 1e-3))))
     return k * n / dt, threads, "port", \
-        f"{k} sampled targets x all {n} sources (restated reference brute force), {dt:.1f} s"
+        f"{k} sampled targets x all {n} sources (restated reference brute force, softened law as the GPU arm), {dt:.1f} s"
 
 
-def cpu_config1_seconds(bodies, steps, dt):
-    """Seconds for `steps` whole updates (accelerate + integrate) of the reference CPU brute
-    force on all host cores: Sim::update (sim.cpp:307-313, Solver::update solver.h:59) over
-    CpuBruteForceSolver -- the reference's own build where present, else its restatement."""
+def cpu_config1_seconds(bodies, steps, dt, eps2):
+    """Seconds for `steps` whole updates (accelerate + integrate) of the reference's CPU
+    brute force on all host cores: Sim::update (sim.cpp:307-313, Solver::update
+    solver.h:59) over CpuBruteForceSolver, restated (speed build), with the GPU arm's
+    softened law."""
     from oracle import oracle as O
     threads = O.threads()
-    if O.ref_available():
-        t0 = time.perf_counter()
-        O.ref_brute_force(bodies, 1.0, steps=steps, dt=dt, nthreads=threads)
-        return time.perf_counter() - t0, threads, "reference (CpuBruteForceSolver, reference law)"
-    b = bodies
+    b = np.ascontiguousarray(bodies, np.float32).copy()
+    tg = np.arange(len(b), dtype=np.int64)
     t0 = time.perf_counter()
     for _ in range(steps):
-        b = O.integrate(O.brute_force(b, 1.0, nthreads=threads), dt, 10000.0, False)
-    return time.perf_counter() - t0, threads, "port (restated CpuBruteForceSolver + integrate)"
+        b[:, 8:11] = O.brute_force_targets(b, 1.0, tg, nthreads=threads, law=O.LAW_SOFTENED, eps2=eps2, timing=True)
+        b = O.integrate(b, dt, 10000.0, False)
+    return time.perf_counter() - t0, threads, "port (restated CpuBruteForceSolver + integrate, softened law)"
 
 
-def cpu_barnes_hut_rate(bodies, size, theta):
-    """Seconds per step of the restated reference CpuBarnesHutSolver (serial tree build +
-    parallel traversal, cpu_barnes_hut.h:22-44) on all host cores."""
+def cpu_barnes_hut_rate(bodies, size, theta, eps2):
+    """Seconds per step of the reference's CpuBarnesHutSolver (serial tree build + parallel
+    traversal, cpu_barnes_hut.h:22-44), restated (speed build), with the GPU arm's softened
+    law, on all host cores."""
     from oracle import oracle as O
     threads = O.threads()
     t0 = time.perf_counter()
-    O.barnes_hut(bodies, size, theta, 1.0, nthreads=threads)
+    O.barnes_hut(bodies, size, theta, 1.0, nthreads=threads, law=O.LAW_SOFTENED, eps2=eps2, timing=True)
     return time.perf_counter() - t0, threads
 
 
@@ -415,6 +413,75 @@ def bench_compensated(torch, stream, flush, native, bodies, args, fp32_value, fp
     return out
 
 
+# Barnes-Hut opening parameters, in the reference's convention (accept when
+# |com - x| > size * theta, bhtree.cpp:117-125): conventional theta = 1 / reference theta.
+BH_THETAS = (("theta_0.5", 0.5), ("theta_0.75", 0.75), ("theta_conventional_0.5", 2.0),
+             ("theta_conventional_0.75", 4.0 / 3.0))
+# compulsory HBM bytes per body of the build (byte model): bbox 16, Morton 16 + 8,
+# sort 7 passes x 24, permute 32, tree ~56 per internal node, COM ~48 per node
+BUILD_BYTES_PER_BODY = 16 + 24 + 7 * 24 + 32 + 56 + 48
+
+
+def bh_run(torch, stream, flush, native, ctx, bodies, p, steps, warmup, a64, tg, fp32_peak, hbm):
+    """One Barnes-Hut configuration: the error of the first accelerate against the FP64 sums
+    on the sampled targets, then `steps` timed update steps and the stage times."""
+    n = len(bodies)
+    ctx.upload_bodies(bodies)
+    ctx.accelerate(p)
+    err = rel_stats(ctx.download_bodies()[tg, 8:11], a64)
+    stats = ctx.bh_stats()
+    for _ in range(warmup):
+        ctx.update(p, 1)
+    torch.cuda.synchronize()
+    ms = timed_steps(torch, stream, flush, lambda: ctx.update(p, 1), steps)
+    stage = []
+    for _ in range(3):
+        ctx.update(p, 1)
+        stage.append(ctx.bh_stage_ms())
+    build_ms = statistics.mean(s[0] for s in stage)
+    walk_ms = statistics.mean(s[1] for s in stage)
+    ms_step = sum(ms) / steps
+    inter = stats["interactions"]
+    return {
+        "steps_per_s": 1e3 / ms_step, "ms_per_step": ms_step, "body_steps_per_s": n * 1e3 / ms_step,
+        "interactions_per_body": inter / n, "tree_cells": stats["cells"],
+        "err_vs_fp64": dict(err, targets=len(tg)),
+        "stage_ms": {"build": build_ms, "traversal": walk_ms, "integrate_and_rest": ms_step - build_ms - walk_ms,
+                     "source": "nbody_cuda_bh_stage_ms (CUDA events), mean of 3 steps"},
+        "roofline": {
+            "build": {"bound": "hbm", "achieved": n * BUILD_BYTES_PER_BODY / (build_ms * 1e-3) / 1e9, "peak": hbm,
+                      "unit": "GB/s", "frac": n * BUILD_BYTES_PER_BODY / (build_ms * 1e-3) / 1e9 / hbm,
+                      "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                      "bytes_model": f"{BUILD_BYTES_PER_BODY} B/body compulsory"},
+            "traversal": {"bound": "fp32 (interactions at 20 flop each)",
+                          "achieved": FLOP_PER_PAIR * inter / (walk_ms * 1e-3) / 1e12, "peak": fp32_peak,
+                          "unit": "TFLOP/s", "frac": FLOP_PER_PAIR * inter / (walk_ms * 1e-3) / 1e12 / fp32_peak,
+                          "peak_source": "measured FFMA/FFMA2 chains (nbody_cuda_calibrate_fp32)",
+                          "interactions_per_s": inter / (walk_ms * 1e-3)},
+        },
+    }
+
+
+def energy_drift(ctx, native, bodies, p, steps):
+    """Relative energy drift and momentum drift of `steps` update steps from `bodies`, from
+    nbody_cuda_energy (FP32 pair terms, exact tile folds, FP64 totals) at both ends."""
+    ctx.upload_bodies(bodies)
+    e0 = ctx.energy(p)
+    t0 = time.perf_counter()
+    ctx.update_graph(p, steps)
+    ctx.synchronize()
+    run_s = time.perf_counter() - t0
+    e1 = ctx.energy(p)
+    E0, E1 = e0["kinetic"] + e0["potential"], e1["kinetic"] + e1["potential"]
+    m = bodies[:, 7].astype(np.float64)
+    pscale = float(np.sum(m * np.linalg.norm(bodies[:, 4:7].astype(np.float64), axis=1)))
+    return {"steps": steps, "run_s": run_s, "energy_start": E0, "energy_end": E1,
+            "energy_drift": (E1 - E0) / abs(E0),
+            "momentum_drift": float(np.linalg.norm(e1["momentum"] - e0["momentum"]) / pscale),
+            "momentum_scale": "sum_i m_i |v_i| at the start",
+            "diagnostics": "nbody_cuda_energy: FP32 pair terms, tile sums folded exactly, FP64 totals"}
+
+
 def bench_bh16m(torch, stream, flush, native, scenes, args):
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs", 6800.0)
@@ -422,69 +489,59 @@ def bench_bh16m(torch, stream, flush, native, scenes, args):
     b = scenes.disk_halo()
     gen_s = time.perf_counter() - t0
     n = len(b)
+    eps2 = 0.005 ** 2
+    tg = np.random.default_rng(5).choice(n, 4096, replace=False)
     res = {"n_bodies": n, "workload": "exponential disk 12,000,000 (R_d=3, z_0=0.3, circular v) + Hernquist "
                                       "halo 4,777,216 (a=10, m_halo = 5 m_disk), eps=0.005, dt=2.5e-4, "
                                       "FP32 tree forces + compensated integration, auto power-of-two root box",
-           "generate_s": gen_s, "theta_convention": "reference (accept when |com-x| > size*theta)"}
+           "generate_s": gen_s,
+           "theta_convention": "keys theta_X use the reference's convention (accept when |com-x| > size*X, "
+                               "bhtree.cpp:117-125); theta_conventional_X is the usual one (accept when "
+                               "size/|com-x| < X), i.e. reference theta 1/X",
+           "walks": {"target": "every target applies exactly the cells the reference's walk accepts for it",
+                     "group": "one walk per 128 Morton-consecutive targets (split at the 3 largest Morton jumps), "
+                              "cells accepted for a whole sub-group, interaction lists; each target's sources "
+                              "refine its reference set"},
+           "err_metric": "|a - a_fp64| / |a_fp64| of the first accelerate, 4096 sampled targets; FP64 = GPU FP64 "
+                         "direct sum (nbody_cuda_accel_sampled)"}
+    steps = max(5, args.steps)
     with native.Context() as ctx:
         ctx.set_stream(stream.cuda_stream)
         fp32_peak = max(ctx.calibrate_fp32())
-        for theta in (0.5, 0.75):
-            ctx.upload_bodies(b)
-            p = native.params(mode=native.MODE_NLOGN, theta=theta, law=native.LAW_SOFTENED, eps2=0.005 ** 2,
-                              dt=2.5e-4, size=0.0, tree_box=1, precision=native.PREC_COMPENSATED)
-            for _ in range(args.warmup):
-                ctx.update(p, 1)
-            torch.cuda.synchronize()
-            steps = max(5, args.steps)
-            ms = timed_steps(torch, stream, flush, lambda: ctx.update(p, 1), steps)
-            # the two stages of the accelerate, from the library's own stream events (one
-            # step at a time, after the timed region)
-            stage = []
-            for _ in range(3):
-                ctx.update(p, 1)
-                stage.append(ctx.bh_stage_ms())
-            build_ms = statistics.mean(s[0] for s in stage)
-            walk_ms = statistics.mean(s[1] for s in stage)
-            ctx.accelerate(p)
-            stats = ctx.bh_stats()
-            ms_step = sum(ms) / steps
-            # compulsory HBM bytes per body of the build (byte model): bbox 16, Morton 16 + 8,
-            # sort 7 passes x 24, permute 32, tree ~56 per internal node, COM ~48 per node
-            build_bpb = 16 + 24 + 7 * 24 + 32 + 56 + 48
-            inter = stats["interactions"]
-            res[f"theta_{theta}"] = {
-                "steps_per_s": 1e3 / ms_step, "ms_per_step": ms_step, "body_steps_per_s": n * 1e3 / ms_step,
-                "interactions": inter, "interactions_per_body": inter / n,
-                "warp_cell_visits": stats["visits"], "tree_cells": stats["cells"],
-                "stage_ms": {"build": build_ms, "traversal": walk_ms,
-                             "integrate_and_rest": ms_step - build_ms - walk_ms,
-                             "source": "nbody_cuda_bh_stage_ms (CUDA events), mean of 3 steps"},
-                "roofline": {
-                    "build": {"bound": "hbm", "achieved": n * build_bpb / (build_ms * 1e-3) / 1e9, "peak": hbm,
-                              "unit": "GB/s", "frac": n * build_bpb / (build_ms * 1e-3) / 1e9 / hbm,
-                              "peak_source": "MEASURED_PEAKS.json hbm_gbs",
-                              "bytes_model": f"{build_bpb} B/body compulsory"},
-                    "traversal": {"bound": "issue (control flow of the walk; cells and bodies are L1/L2 hits)",
-                                  "achieved": FLOP_PER_PAIR * inter / (walk_ms * 1e-3) / 1e12, "peak": fp32_peak,
-                                  "unit": "TFLOP/s", "frac": FLOP_PER_PAIR * inter / (walk_ms * 1e-3) / 1e12 / fp32_peak,
-                                  "peak_source": "measured FFMA/FFMA2 chains (nbody_cuda_calibrate_fp32)",
-                                  "flop_model": f"{FLOP_PER_PAIR} flop per interaction, as the direct sum",
-                                  "interactions_per_s": inter / (walk_ms * 1e-3)},
-                },
-            }
-        p = native.params(mode=native.MODE_NLOGN, theta=0.5, law=native.LAW_SOFTENED, eps2=0.005 ** 2,
+        ctx.upload_bodies(b)
+        a64 = ctx.accel_sampled(native.params(law=native.LAW_SOFTENED, eps2=eps2, precision=native.PREC_FP64), tg)
+        for key, theta in BH_THETAS:
+            entry = {"theta_reference": theta, "theta_conventional": 1.0 / theta, "per_walk": {}}
+            for wname, walk in (("target", native.WALK_TARGET), ("group", native.WALK_GROUP)):
+                p = native.params(mode=native.MODE_NLOGN, theta=theta, law=native.LAW_SOFTENED, eps2=eps2,
+                                  dt=2.5e-4, size=0.0, tree_box=1, precision=native.PREC_COMPENSATED, walk=walk)
+                entry["per_walk"][wname] = bh_run(torch, stream, flush, native, ctx, b, p, steps, args.warmup,
+                                                  a64, tg, fp32_peak, hbm)
+            # the headline fields: the faster walk (the group walk is at least as accurate)
+            fast = min(entry["per_walk"], key=lambda w: entry["per_walk"][w]["ms_per_step"])
+            entry = {**entry, "walk": fast, **entry["per_walk"][fast]}
+            res[key] = entry
+        # 100 steps (config 5) at conventional theta 0.5 and at reference theta 0.5, the faster
+        # walk each, energy and momentum drift from the diagnostics at both ends
+        res["drift_100_steps"] = {}
+        for key in ("theta_conventional_0.5", "theta_0.5"):
+            theta = res[key]["theta_reference"]
+            walk = native.WALK_GROUP if res[key]["walk"] == "group" else native.WALK_TARGET
+            p = native.params(mode=native.MODE_NLOGN, theta=theta, law=native.LAW_SOFTENED, eps2=eps2, dt=2.5e-4,
+                              size=0.0, tree_box=1, precision=native.PREC_COMPENSATED, walk=walk)
+            res["drift_100_steps"][key] = dict(energy_drift(ctx, native, b, p, 100), walk=res[key]["walk"])
+        p = native.params(mode=native.MODE_NLOGN, theta=0.5, law=native.LAW_SOFTENED, eps2=eps2,
                           dt=2.5e-4, size=0.0, tree_box=1, precision=native.PREC_COMPENSATED)
         res["transfer"] = bench_transfer(torch, native, ctx, b, p)
     # one full step of the restated CPU Barnes-Hut on the same bodies, on all host cores:
     # the reference's fixed root box (centred at the origin), made a power of two that holds
-    # every body
+    # every body; the GPU arm's softened law
     size = float(2.0 ** np.ceil(np.log2(2.0 * float(np.abs(b[:, :3]).max()))))
-    cpu_s, cores = cpu_barnes_hut_rate(b, size, 0.5)
+    cpu_s, cores = cpu_barnes_hut_rate(b, size, 0.5, eps2)
     res["cpu_reference_bh"] = {
         "theta": 0.5, "step_s": cpu_s, "cores": cores, "body_steps_per_s": n / cpu_s,
         "kind": "port (restated CpuBarnesHutSolver, cpu_barnes_hut.h:22-44: serial tree build, "
-                "parallel traversal)",
+                "parallel traversal; softened law as the GPU arm)",
         "root_box": f"centred at the origin, edge {size:g}",
         "gpu_speedup": cpu_s / (res["theta_0.5"]["ms_per_step"] * 1e-3)}
     return res
@@ -706,51 +763,100 @@ def bench_small_configs(torch, stream, flush, native, scenes):
         torch.cuda.synchronize()
         ms = timed_steps(torch, stream, flush, lambda: ctx.update(p, 100), 1)[0]
         ms_graph = timed_steps(torch, stream, flush, lambda: ctx.update_graph(p, 100), 1)[0]
-    cpu_s, cores, kind = cpu_config1_seconds(b, 100, 1e-3)
+    # FP64 error of the first accelerate (all 4096 bodies, CPU FP64 oracle)
+    from oracle import oracle as O
+    a64 = O.direct_f64(b[:, [0, 1, 2, 7]], 1.0, float(np.float32(1e-4)), O.LAW_SOFTENED)
+    with native.Context() as ctx:
+        ctx.upload_bodies(b)
+        ctx.accelerate(p)
+        err = rel_stats(ctx.download_bodies()[:, 8:11], a64)
+    cpu_s, cores, kind = cpu_config1_seconds(b, 100, 1e-3, 1e-4)
     out["config1_plummer_4096"] = {"steps": 100, "ms_eager": ms, "ms_graph": ms_graph,
                                    "body_steps_per_s": 4096 * 100 / (min(ms, ms_graph) * 1e-3),
+                                   "err_vs_fp64": dict(err, targets=4096),
                                    "cpu_100_steps_s": cpu_s, "cpu_body_steps_per_s": 4096 * 100 / cpu_s,
                                    "cpu_cores": cores, "cpu_kind": kind}
-    # config 2: two Plummer spheres, BH theta 0.5 (reference convention), 200 steps
+    # config 2: two Plummer spheres of 131072, eps 0.01, dt 5e-4, 200 steps, the reference's
+    # fixed 64 box; reference theta 0.5 and conventional theta 0.5, both walks; FP64 errors
+    # of the first accelerate on 4096 sampled targets (CPU FP64 oracle)
     b = scenes.two_plummer(131072)
-    p = native.params(mode=native.MODE_NLOGN, theta=0.5, dt=5e-4, eps2=1e-4, law=native.LAW_SOFTENED,
-                      size=64.0)
-    with native.Context() as ctx:
-        ctx.set_stream(stream.cuda_stream)
-        ctx.upload_bodies(b)
-        ctx.update(p, 3)
-        ctx.update_graph(p, 3)
-        torch.cuda.synchronize()
-        ms_eager = timed_steps(torch, stream, flush, lambda: ctx.update(p, 200), 1)[0]
-        ms_graph = timed_steps(torch, stream, flush, lambda: ctx.update_graph(p, 200), 1)[0]
-        stats = ctx.bh_stats()
-    ms = min(ms_eager, ms_graph)
-    cpu_s, cores = cpu_barnes_hut_rate(b, 64.0, 0.5)
-    out["config2_two_plummer_bh"] = {"n_bodies": len(b), "steps": 200, "ms": ms, "ms_eager": ms_eager,
-                                     "ms_graph": ms_graph, "steps_per_s": 200 / (ms * 1e-3),
-                                     "body_steps_per_s": len(b) * 200 / (ms * 1e-3),
-                                     "interactions_per_body": stats["interactions"] / len(b),
-                                     "cpu_reference_bh_step_s": cpu_s, "cpu_cores": cores,
-                                     "cpu_kind": "port (restated CpuBarnesHutSolver, serial build)"}
+    tg = np.random.default_rng(2).choice(len(b), 4096, replace=False)
+    a64 = O.direct_f64(b[:, [0, 1, 2, 7]], 1.0, float(np.float32(1e-4)), O.LAW_SOFTENED, targets=tg)
+    c2 = {"n_bodies": len(b), "steps": 200, "err_metric": "|a - a_fp64| / |a_fp64|, 4096 sampled targets"}
+    for key, theta in (("theta_0.5", 0.5), ("theta_conventional_0.5", 2.0)):
+        entry = {"theta_reference": theta, "per_walk": {}}
+        for wname, walk in (("target", native.WALK_TARGET), ("group", native.WALK_GROUP)):
+            p = native.params(mode=native.MODE_NLOGN, theta=theta, dt=5e-4, eps2=1e-4, law=native.LAW_SOFTENED,
+                              size=64.0, walk=walk)
+            with native.Context() as ctx:
+                ctx.set_stream(stream.cuda_stream)
+                ctx.upload_bodies(b)
+                ctx.accelerate(p)
+                err = rel_stats(ctx.download_bodies()[tg, 8:11], a64)
+                stats = ctx.bh_stats()
+                ctx.update(p, 3)
+                ctx.update_graph(p, 3)
+                torch.cuda.synchronize()
+                ms_eager = timed_steps(torch, stream, flush, lambda: ctx.update(p, 200), 1)[0]
+                ms_graph = timed_steps(torch, stream, flush, lambda: ctx.update_graph(p, 200), 1)[0]
+            ms = min(ms_eager, ms_graph)
+            entry["per_walk"][wname] = {"ms": ms, "ms_eager": ms_eager, "ms_graph": ms_graph,
+                                        "steps_per_s": 200 / (ms * 1e-3),
+                                        "body_steps_per_s": len(b) * 200 / (ms * 1e-3),
+                                        "interactions_per_body": stats["interactions"] / len(b),
+                                        "err_vs_fp64": dict(err, targets=len(tg))}
+        fast = min(entry["per_walk"], key=lambda w: entry["per_walk"][w]["ms"])
+        c2[key] = {**entry, "walk": fast, **entry["per_walk"][fast]}
+    cpu_s, cores = cpu_barnes_hut_rate(b, 64.0, 0.5, float(np.float32(1e-4)))
+    c2.update({"cpu_reference_bh_step_s": cpu_s, "cpu_cores": cores,
+               "cpu_kind": "port (restated CpuBarnesHutSolver, serial build, softened law), reference theta 0.5"})
+    out["config2_two_plummer_bh"] = c2
     return out
 
 
 def bench_reference(args):
+    """The reference's CPU brute force (CpuBruteForceSolver::accelerate, cpu_brute_force.h:17-43,
+    restated in the oracle, speed build) with the GPU arm's softened law, on all host cores.
+    A step is a bounded sample of the workload: k targets spread over the N bodies, each
+    summed against all N sources and integrated (physics.h:60-70); body-steps/s counts the k.
+    ms_per_step is that sample's own time, so steps x ms_per_step is the timed region."""
     rank, world, _ = env_rank()
     if rank != 0:
         return None
     from nbody_gb300 import scenes
+    from oracle import oracle as O
     bodies = scenes.uniform_cube(N, seed=1003)
-    per_step = []
-    info = None
-    for k in range(args.warmup + args.steps):
-        rate, cores, kind, sample = cpu_brute_force_rate(bodies, seconds=args.cpu_seconds / 2)
-        info = (cores, kind, sample)
-        if k >= args.warmup:
-            per_step.append(float(N) * N / rate)    # seconds for one step: N^2 pairs at `rate` pairs/s
-    total = sum(per_step)
-    value = N * args.steps / total
-    cores, kind, sample = info
+    threads = O.threads()
+    eps2 = EPS * EPS
+    target_s = max(0.5, args.cpu_seconds / 5)
+
+    def step(tg):
+        acc = O.brute_force_targets(bodies, 1.0, tg, nthreads=threads, law=O.LAW_SOFTENED, eps2=eps2, timing=True)
+        sub = bodies[tg].copy()
+        sub[:, 8:11] = acc
+        return O.integrate(sub, DT, 10000.0, False)
+
+    k = 256
+    while True:                 # size a step to about target_s seconds
+        tg = np.linspace(0, N - 1, k).astype(np.int64)
+        t0 = time.perf_counter()
+        step(tg)
+        dt = time.perf_counter() - t0
+        if dt >= 0.5 * target_s or k >= N:
+            break
+        k = min(N, int(k * min(8.0, max(1.5, target_s / max(dt, 1e-3)))))
+    tg = np.linspace(0, N - 1, k).astype(np.int64)
+    for _ in range(args.warmup):
+        step(tg)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step(tg)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = k * args.steps / total
+    sample = (f"{k} targets spread over the {N} bodies, each against all {N} sources (restated reference "
+              f"brute force, softened law as the GPU arm, speed build) and integrated, per step")
     return {
         "impl": "reference",
         "metric": METRIC,
@@ -765,11 +871,11 @@ def bench_reference(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded Philox): uniform unit cube, log-normal masses",
-        "config": {"workload": WORKLOAD, "n_bodies": N, "eps": EPS, "dt": DT,
-                   "note": "the reference CPU brute force uses its own radius-cutoff law (no softening); "
-                           "same pair count and arithmetic class"},
-        "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": cores, "kind": kind,
-                         "sample": sample + " per step; body-steps/s = pairs/s / N"},
+        "config": {"workload": WORKLOAD, "n_bodies": N, "eps": EPS, "dt": DT, "law": "softened",
+                   "same_config": True, "bodies_per_step": k,
+                   "note": "the GPU arm's workload and law; a step is a bounded sample of k of its N bodies"},
+        "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                         "sample": sample, "pairs_per_s": k * N * args.steps / total},
         "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
