@@ -19,12 +19,13 @@
 //   - the source range can be split into `jsplit` chunks (blockIdx.y) so that the grid
 //     fills the 152 SMs evenly; chunk partials go to a scratch array and are summed in
 //     a fixed order (deterministic) by reduce_partials or the fused integrate.
-//   - summation: each 256-source tile is summed in FP32 from zero, and the tile sums are
-//     folded into an (S, C) pair per component by an error-free TwoSum, so S + C is the
-//     sum of the tile sums to about 2^-44 of their magnitude. A chunk leaves (S, C); the
+//   - summation: each run of 1024 sources (4 tiles; one 256-source tile when n < 65536)
+//     is summed in FP32 from zero, and the run sums are folded into an (S, C) pair per
+//     component by an error-free TwoSum, so S + C is the sum of the run sums to about
+//     2^-44 of their magnitude. A chunk leaves (S, C); the
 //     result is G * float(sum over chunks of S + C, as a double-float sum; direct.cuh
-//     combine_partials). The tiles are the same 256
-//     sources for every kernel shape and split, so the result does not depend on the
+//     combine_partials). The runs are the same sources
+//     for every kernel shape and split, so the result does not depend on the
 //     launch shape (up to a rounding tie of the last fold), and it is more accurate than
 //     one FP32 running sum over all N sources.
 #include <algorithm>
@@ -126,7 +127,7 @@ namespace nbg
                        const float4* __restrict__ vel_radius, // SoA radius source (CUTOFF)
                        float4* __restrict__ out,              // acc (SoA) / partials
                        float* __restrict__ body_out,          // AoS Body array to write acc
-                       const int n, const int chunk, const float G, const float eps2,
+                       const int n, const int chunk, const int fold, const float G, const float eps2,
                        unsigned* __restrict__ err)
     {
         constexpr int P = T / 2;
@@ -139,7 +140,7 @@ namespace nbg
         // compensation C; one column per thread, so a warp's accesses are conflict-free.
         // Shared memory rather than registers: the 4 x 256 shape runs three CTAs per SM
         // only within 85 registers.
-        extern __shared__ __align__(16) float2 fold[];
+        extern __shared__ __align__(16) float2 fold_sc[];
 
         const int tid = threadIdx.x;
         const int base = blockIdx.x * (BLOCK * T);
@@ -195,7 +196,7 @@ namespace nbg
             ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
 #pragma unroll
             for (int r = 0; r < 6; ++r)
-                fold[(6 * p + r) * BLOCK + tid] = make_float2(0.f, 0.f);
+                fold_sc[(6 * p + r) * BLOCK + tid] = make_float2(0.f, 0.f);
         }
 
         int failed_at = -1;
@@ -252,13 +253,15 @@ namespace nbg
                         interact2<LAW, PACKED>(sx, sy, sz, sm, nx[p], ny[p], nz[p], lim[p], ax[p], ay[p], az[p]);
                 }
             }
-            // fold this tile's sums into (S, C) and start the next tile from zero
+            // every `fold` tiles (and after the chunk's last), fold the running sums into
+            // (S, C) and start again from zero; chunks start on fold boundaries
+            if ((t + 1) % fold == 0 || t + 1 == ntiles)
 #pragma unroll
             for (int p = 0; p < P; ++p)
             {
-                fold_tile(&fold[(6 * p) * BLOCK + tid], BLOCK, ax[p]);
-                fold_tile(&fold[(6 * p + 1) * BLOCK + tid], BLOCK, ay[p]);
-                fold_tile(&fold[(6 * p + 2) * BLOCK + tid], BLOCK, az[p]);
+                fold_tile(&fold_sc[(6 * p) * BLOCK + tid], BLOCK, ax[p]);
+                fold_tile(&fold_sc[(6 * p + 1) * BLOCK + tid], BLOCK, ay[p]);
+                fold_tile(&fold_sc[(6 * p + 2) * BLOCK + tid], BLOCK, az[p]);
                 ax[p] = ay[p] = az[p] = make_float2(0.f, 0.f);
             }
             __syncthreads();
@@ -283,8 +286,8 @@ namespace nbg
 #pragma unroll
             for (int c = 0; c < 3; ++c)
             {
-                S[c] = fold[(6 * p + c) * BLOCK + tid];
-                Cc[c] = fold[(6 * p + 3 + c) * BLOCK + tid];
+                S[c] = fold_sc[(6 * p + c) * BLOCK + tid];
+                Cc[c] = fold_sc[(6 * p + 3 + c) * BLOCK + tid];
             }
 #pragma unroll
             for (int h = 0; h < 2; ++h)
@@ -345,8 +348,14 @@ namespace nbg
         constexpr int kTile = 256;
         constexpr int kStages = 3;
 
-        using KernelFn = void (*)(const float4*, const float4*, float4*, float*, int, int, float,
+        using KernelFn = void (*)(const float4*, const float4*, float4*, float*, int, int, int, float,
                                   float, unsigned*);
+        // Sources per exact fold of the running sums: 4 tiles (1024) from n = 65536 up, where
+        // folding after every tile cost 3 % of the FMA pipe's time at n = 2^20; 1 tile below,
+        // where the split gives small systems chunks of a single tile. A function of n only,
+        // so every shape at a given n folds at the same sources.
+        constexpr int kFoldTiles = 4;
+        constexpr size_t kFoldMinN = 65536;
 
         struct Variant
         {
@@ -484,15 +493,18 @@ namespace nbg
                 best_js = js;
             }
         }
-        // Chunks hold whole tiles, so the last chunk is the only ragged one.
+        // Chunks hold whole fold units, so the last chunk is the only ragged one.
+        const int fold = n >= kFoldMinN ? kFoldTiles : 1;
+        const size_t unit = static_cast<size_t>(kTile) * fold;
         size_t chunk = (n + best_js - 1) / best_js;
-        chunk = (chunk + kTile - 1) / kTile * kTile;
+        chunk = (chunk + unit - 1) / unit * unit;
         const size_t js = std::max<size_t>(1, (n + chunk - 1) / chunk);
 
         plan.variant = chosen;
         plan.T = v.T;
         plan.block = v.block;
         plan.tile = kTile;
+        plan.fold = fold;
         plan.jsplit = static_cast<int>(js);
         plan.chunk = static_cast<int>(chunk);
         plan.grid_x = static_cast<int>(tb);
@@ -516,7 +528,7 @@ namespace nbg
         float4* out = plan.jsplit > 1 ? scratch : acc;
         allow_dynamic_smem(fn, v.fold_bytes);
         fn<<<grid, v.block, v.fold_bytes, stream>>>(src, vel_radius, out, plan.aos ? body_out : nullptr, n,
-                                                    plan.chunk, G, eps2, err);
+                                                    plan.chunk, plan.fold, G, eps2, err);
         ++*launches;
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess || plan.jsplit <= 1 || !reduce)

@@ -17,7 +17,8 @@ namespace nbg
         int block;      // threads per CTA
         int tile;       // sources per shared-memory tile
         int jsplit;     // source chunks (grid.y); >1 means partials + a fixed-order sum
-        int chunk;      // sources per chunk (a multiple of tile)
+        int chunk;      // sources per chunk (a multiple of tile * fold)
+        int fold;       // tiles per exact fold of the running sums (a function of n only)
         int grid_x;     // target blocks
         int law;
         bool aos;
@@ -41,6 +42,7 @@ namespace nbg
                                                        const int js, const int n, const int i, const float G)
     {
         float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
+#pragma unroll 4
         for (int c = 0; c < js; ++c)
         {
             const size_t k = 2 * static_cast<size_t>(c) * n + i;

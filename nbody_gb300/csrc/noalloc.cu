@@ -157,7 +157,8 @@ extern "C" int nbody_cuda_dev_accel_soa_noalloc(const void* pos_mass, const void
     {
         const size_t js = std::max<size_t>(1, kNoAllocPartials / (2 * n));
         size_t chunk = (n + js - 1) / js;
-        chunk = (chunk + plan.tile - 1) / plan.tile * plan.tile;
+        const size_t unit = static_cast<size_t>(plan.tile) * plan.fold;
+        chunk = (chunk + unit - 1) / unit * unit;
         plan.chunk = static_cast<int>(chunk);
         plan.jsplit = static_cast<int>((n + chunk - 1) / chunk);
     }
