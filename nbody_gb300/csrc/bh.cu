@@ -59,10 +59,9 @@ namespace nbg
         // group walk: warps per CTA, list entries and stacked parent cells per warp (the
         // stack grows by at most 28 parents per tree level, 22 levels: 616 < 768)
         constexpr int kListWarps = 4;
-        constexpr int kListCap = 256;       // full-list entries
-        constexpr int kPartCap = 128;       // partial-list entries
+        constexpr int kListCap = 256;       // interaction-list entries per warp
         constexpr int kGroupStack = 768;
-        constexpr int kSubGroups = 4;       // sub-groups per group (a 4-bit mask per stacked cell)
+        constexpr int kRuns = 4;            // runs (own acceptance boxes) per group
         constexpr int kBboxBlocks = 1024;
         constexpr int kBboxVals = 8;    // min x y z, max x y z, max |m|, max |x|
         constexpr int kMomThreads = 1024;
@@ -1127,13 +1126,11 @@ namespace nbg
     // ------------------------------------------------------------------------------------
     // 7b. group walk with interaction lists (walk = NBODY_WALK_GROUP)
     // ------------------------------------------------------------------------------------
-    // One list source applied to two targets (negated positions): the direct sum's packed
-    // interaction, 3 FADD2 + 3 FFMA2 + 2 MUFU.RSQ + 3 FMUL2 + 3 FFMA2. MASKED: a half
-    // whose target does not take the source gets s = 0, which adds exactly zero.
-    template <int LAW, bool MASKED>
+    // One list source applied to two targets (negated positions), both taking it: the direct
+    // sum's packed interaction, 3 FADD2 + 3 FFMA2 + 2 MUFU.RSQ + 3 FMUL2 + 3 FFMA2.
+    template <int LAW>
     __device__ __forceinline__ void apply_list2(const float2 npx, const float2 npy, const float2 npz, const float2 lim,
-                                                const float4 s, const bool take_a, const bool take_b, float2& ax,
-                                                float2& ay, float2& az)
+                                                const float4 s, float2& ax, float2& ay, float2& az)
     {
         const float2 dx = add2(f2(s.x), npx), dy = add2(f2(s.y), npy), dz = add2(f2(s.z), npz);
         float2 r2 = (LAW == NBODY_LAW_SOFTENED) ? fma2(dx, dx, lim) : mul2(dx, dx);
@@ -1147,12 +1144,7 @@ namespace nbg
         }
         const float2 inv2 = mul2(inv, inv);
         const float2 mi = mul2(f2(s.w), inv);
-        float2 sc = mul2(mi, inv2);
-        if (MASKED)
-        {
-            sc.x = take_a ? sc.x : 0.f;
-            sc.y = take_b ? sc.y : 0.f;
-        }
+        const float2 sc = mul2(mi, inv2);
         ax = fma2(dx, sc, ax);
         ay = fma2(dy, sc, ay);
         az = fma2(dz, sc, az);
@@ -1172,29 +1164,30 @@ namespace nbg
 
     // A warp serves 64 Q Morton-consecutive targets (lane l holds targets 64 Q t + 32 h + l,
     // h < 2Q, as Q packed pairs) with one walk of the tree, the interaction-list walk of GPU
-    // tree codes (Barnes 1990's grouping; Bonsai, Bedorf et al. 2012).
+    // tree codes (Barnes 1990's grouping; Bonsai, Bedorf et al. 2012): the walk decides each
+    // cell once for the whole group and appends the sources it yields -- accepted cells as
+    // (com, mass), leaves and the bodies of opened buckets as (x, m) -- to an interaction list
+    // in shared memory, which every kListCap entries is applied to every target of the group
+    // with the direct sum's packed loop: no selection and no per-target test.
     //
-    // Sub-groups. The targets are split at the kSubGroups - 1 largest jumps of their Morton
-    // codes (the smallest common prefixes of neighbours) into sub-groups, each with its own
-    // bounding box: a run that crosses from one cell of the tree into a distant one (at the
-    // end of a top-level octant the curve jumps across the whole system) would otherwise
-    // have a box spanning everything between, and open every cell there down to its leaves.
+    // The acceptance box. The group is split at the NSG - 1 largest jumps of its Morton codes
+    // (the smallest common prefixes of neighbours) into runs, each with its own bounding box,
+    // and a cell is accepted only when every run's box lies beyond its opening distance;
+    // otherwise it is opened for the whole group. One box over the group would be wrong in
+    // shape: a run that crosses from one cell of the tree into a distant one (at the end of a
+    // top-level octant the curve jumps across the whole system) has a box spanning everything
+    // between, which opens every cell there down to its leaves. Accepting per run instead
+    // (some runs taking a cell, the others its children) was measured too: half the list then
+    // applies to only some targets, and the walk took 54 against 45 ms at 16.8M bodies.
     //
-    // The walk decides each cell once per sub-group and appends the sources it yields --
-    // accepted cells as (com, mass), leaves and the bodies of opened buckets as (x, m) --
-    // to an interaction list in shared memory, with the sub-groups that take each source.
-    // Sources every sub-group takes go to a full list, applied to every target with the
-    // direct sum's packed loop; the rest go to a partial list applied with a per-target
-    // selection. Both are drained when either fills.
-    //
-    // The walk tests up to 32 cells at a time: it pops up to four parent cells, each with
-    // the sub-groups that opened it, from a stack, and lane l tests child l % 8 of parent
-    // l / 8. The stack grows by at most 28 parents per tree level (22 levels: 616 < 768).
+    // The walk tests up to 32 cells at a time: it pops up to four opened parent cells from a
+    // stack, and lane l tests child l % 8 of parent l / 8. The stack grows by at most 28
+    // parents per tree level (22 levels: 616 < kGroupStack).
     //
     // Each target's sources refine the cells the reference's walk accepts for it alone (a
-    // cell opened for its sub-group may be one the target would have accepted), so each
-    // target is summed at least as finely as in the reference, over more interactions.
-    template <int LAW, int Q>
+    // cell opened for the group may be one the target would have accepted), so each target
+    // is summed at least as finely as in the reference, over more interactions.
+    template <int LAW, int Q, int NSG>
     __global__ void __launch_bounds__(kListWarps * 32) traverse_list_kernel(
         const OctNode* __restrict__ nodes, const float4* __restrict__ spm, const float* __restrict__ srad,
         const uint64_t* __restrict__ codes, const uint32_t* __restrict__ order, const int n, const float G,
@@ -1203,21 +1196,15 @@ namespace nbg
     {
         constexpr int H = 2 * Q;                    // target slots per lane
         constexpr int TW = 32 * H;                  // targets per group
-        constexpr int NSG = kSubGroups;
-        __shared__ __align__(16) float4 full_mem[kListWarps][kListCap];
-        __shared__ __align__(16) float4 part_mem[kListWarps][kPartCap];
-        __shared__ unsigned char pmask_mem[kListWarps][kPartCap];
-        __shared__ unsigned stack_mem[kListWarps][kGroupStack];   // cell | sub-group mask << 28
+        static_assert(NSG >= 1 && NSG <= 32, "runs per group");
+        __shared__ __align__(16) float4 list_mem[kListWarps][kListCap];
+        __shared__ int stack_mem[kListWarps][kGroupStack];
         __shared__ __align__(16) float4 box_mem[kListWarps][2 * NSG];
-        __shared__ int cnt_mem[kListWarps][1 << NSG];            // valid targets per sub-group mask
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         const unsigned lt = (1u << lane) - 1u;
-        float4* full = full_mem[warp];
-        float4* part = part_mem[warp];
-        unsigned char* pmask = pmask_mem[warp];
-        unsigned* stk = stack_mem[warp];
+        float4* list = list_mem[warp];
+        int* stk = stack_mem[warp];
         const float4* box = box_mem[warp];
-        const int* cnt_of = cnt_mem[warp];
         unsigned long long inter = 0;               // interactions summed by this warp (uniform)
         unsigned iters = 0;
 
@@ -1230,18 +1217,20 @@ namespace nbg
         for (int tile = next_tile(); static_cast<long long>(tile) * TW < n; tile = next_tile())
         {
             const int t0 = tile * TW;
-            // --- sub-group splits: the NSG - 1 largest Morton jumps between neighbours ---
+            const int nvalid = static_cast<int>(min(static_cast<long long>(TW), static_cast<long long>(n) - t0));
+            // --- runs: split at the NSG - 1 largest Morton jumps between neighbours ---
             unsigned key[H];    // (common prefix bits << 8 | position); 0xffffffff: no boundary
 #pragma unroll
             for (int h = 0; h < H; ++h)
             {
                 const int b = 32 * h + lane;        // boundary between positions b - 1 and b
                 key[h] = 0xffffffffu;
-                if (b > 0 && t0 + b < n)
+                if (b > 0 && b < nvalid)
                     key[h] = (static_cast<unsigned>(__clzll(static_cast<long long>(codes[t0 + b - 1] ^ codes[t0 + b])))
                               << 8) | static_cast<unsigned>(b);
             }
-            int split[NSG - 1];
+            int split[NSG > 1 ? NSG - 1 : 1];
+            split[0] = TW;
 #pragma unroll
             for (int sidx = 0; sidx < NSG - 1; ++sidx)
             {
@@ -1257,9 +1246,8 @@ namespace nbg
                     if (key[h] == m)
                         key[h] = 0xffffffffu;
             }
-            // --- targets, their sub-group bits and the sub-group boxes ---
+            // --- targets and the run boxes ---
             float2 npx[Q], npy[Q], npz[Q], lim[Q], ax[Q], ay[Q], az[Q];
-            unsigned bit[H];
             float4 blo[NSG], bhi[NSG];
 #pragma unroll
             for (int g = 0; g < NSG; ++g)
@@ -1274,19 +1262,17 @@ namespace nbg
 #pragma unroll
                 for (int e = 0; e < 2; ++e)
                 {
-                    const int h = 2 * q + e;
-                    const int pos = 32 * h + lane;
+                    const int pos = 32 * (2 * q + e) + lane;
                     const int k = t0 + pos;
                     const bool valid = k < n;
-                    int sg = 0;
+                    int run = 0;
 #pragma unroll
                     for (int sidx = 0; sidx < NSG - 1; ++sidx)
-                        sg += pos >= split[sidx] ? 1 : 0;
-                    bit[h] = valid ? (1u << sg) : 0u;
+                        run += pos >= split[sidx] ? 1 : 0;
                     const float4 pk = spm[valid ? k : n - 1];
 #pragma unroll
                     for (int g = 0; g < NSG; ++g)
-                        if (valid && sg == g)
+                        if (valid && run == g)
                         {
                             blo[g] = make_float4(fminf(blo[g].x, pk.x), fminf(blo[g].y, pk.y), fminf(blo[g].z, pk.z), 0.f);
                             bhi[g] = make_float4(fmaxf(bhi[g].x, pk.x), fmaxf(bhi[g].y, pk.y), fmaxf(bhi[g].z, pk.z), 0.f);
@@ -1319,27 +1305,7 @@ namespace nbg
                     bhi[g].y = fmaxf(bhi[g].y, __shfl_xor_sync(0xffffffffu, bhi[g].y, o));
                     bhi[g].z = fmaxf(bhi[g].z, __shfl_xor_sync(0xffffffffu, bhi[g].z, o));
                 }
-            // valid targets per sub-group, and the sub-groups that have any (the full mask)
-            int cnt[NSG];
-#pragma unroll
-            for (int g = 0; g < NSG; ++g)
-            {
-                cnt[g] = 0;
-#pragma unroll
-                for (int h = 0; h < H; ++h)
-                    cnt[g] += __popc(__ballot_sync(0xffffffffu, bit[h] == (1u << g)));
-            }
-            unsigned all = 0;
-#pragma unroll
-            for (int g = 0; g < NSG; ++g)
-                all |= cnt[g] > 0 ? (1u << g) : 0u;
-            // the sub-groups present among each target pair's targets, over the warp: a
-            // partial entry none of them takes skips that pair (a uniform branch)
-            unsigned pair_groups[Q];
-#pragma unroll
-            for (int q = 0; q < Q; ++q)
-                pair_groups[q] = __reduce_or_sync(0xffffffffu, bit[2 * q] | bit[2 * q + 1]);
-            __syncwarp();       // the previous group's readers of box/cnt are done
+            __syncwarp();       // the previous group's readers of the boxes are done
             if (lane < 2 * NSG)
             {
                 const int g = lane >> 1;
@@ -1350,82 +1316,51 @@ namespace nbg
                         bv = (lane & 1) ? bhi[gg] : blo[gg];
                 box_mem[warp][lane] = bv;
             }
-            if (lane < (1 << NSG))
-            {
-                int c = 0;
-#pragma unroll
-                for (int g = 0; g < NSG; ++g)
-                    c += ((lane >> g) & 1) ? cnt[g] : 0;
-                cnt_mem[warp][lane] = c;
-            }
             __syncwarp();
 
-            int fn_ = 0, pn = 0;    // entries in the full and partial lists (warp-uniform)
-            // apply both lists to every target of the group, then empty them
+            int ln = 0;     // list entries (warp-uniform)
+            // apply the whole list to every target of the group, then empty it
             auto drain = [&]() {
                 __syncwarp();
 #pragma unroll 2
-                for (int e = 0; e < fn_; ++e)
+                for (int e = 0; e < ln; ++e)
                 {
-                    const float4 s = full[e];
+                    const float4 s = list[e];
 #pragma unroll
                     for (int q = 0; q < Q; ++q)
-                        apply_list2<LAW, false>(npx[q], npy[q], npz[q], lim[q], s, true, true, ax[q], ay[q], az[q]);
+                        apply_list2<LAW>(npx[q], npy[q], npz[q], lim[q], s, ax[q], ay[q], az[q]);
                 }
-                inter += static_cast<unsigned long long>(fn_) * cnt_of[all];
-                for (int e = 0; e < pn; ++e)
-                {
-                    const float4 s = part[e];
-                    const unsigned m = pmask[e];
-#pragma unroll
-                    for (int q = 0; q < Q; ++q)
-                        if (m & pair_groups[q])
-                            apply_list2<LAW, true>(npx[q], npy[q], npz[q], lim[q], s, (m & bit[2 * q]) != 0u,
-                                                   (m & bit[2 * q + 1]) != 0u, ax[q], ay[q], az[q]);
-                    inter += static_cast<unsigned long long>(cnt_of[m]);
-                }
-                fn_ = 0;
-                pn = 0;
+                inter += static_cast<unsigned long long>(ln) * nvalid;
+                ln = 0;
                 __syncwarp();
             };
-            // append one source per flagged lane (mask: the sub-groups taking it; 0: none),
-            // draining first when a list would overflow
-            auto append = [&](const unsigned mask, const float4 src) {
-                const bool to_full = mask != 0u && mask == all;
-                const bool to_part = mask != 0u && mask != all;
-                const unsigned mf = __ballot_sync(0xffffffffu, to_full);
-                const unsigned mp = __ballot_sync(0xffffffffu, to_part);
-                if (fn_ + __popc(mf) > kListCap || pn + __popc(mp) > kPartCap)
+            // append one source per flagged lane, draining first when the list would overflow
+            auto append = [&](const bool take, const float4 src) {
+                const unsigned m = __ballot_sync(0xffffffffu, take);
+                if (ln + __popc(m) > kListCap)
                     drain();
-                if (to_full)
-                    full[fn_ + __popc(mf & lt)] = src;
-                if (to_part)
-                {
-                    const int at = pn + __popc(mp & lt);
-                    part[at] = src;
-                    pmask[at] = static_cast<unsigned char>(mask);
-                }
-                fn_ += __popc(mf);
-                pn += __popc(mp);
+                if (take)
+                    list[ln + __popc(m & lt)] = src;
+                ln += __popc(m);
             };
             // the bodies of an opened bucket (identical codes), 32 at a time
-            auto append_range = [&](const int first, const int last, const unsigned mask) {
+            auto append_range = [&](const int first, const int last) {
                 for (int b0 = first; b0 <= last; b0 += 32)
                 {
                     const int bi = b0 + lane;
                     float4 sb = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (bi <= last)
                         sb = spm[bi];
-                    append(bi <= last && sb.w != 0.f ? mask : 0u, sb);
+                    append(bi <= last && sb.w != 0.f, sb);
                 }
             };
-            // which of the sub-groups in `mask` accept a cell
-            auto accepting = [&](const float4 cm, const float open_r2, const unsigned mask) {
-                unsigned a = 0;
+            // every run's box lies beyond the cell's opening distance (an empty run's box is
+            // inverted, +inf to -inf, and accepts everything)
+            auto accepts = [&](const float4 cm, const float open_r2) {
+                bool a = true;
 #pragma unroll
                 for (int g = 0; g < NSG; ++g)
-                    if (((mask >> g) & 1u) && box_accepts(cm, open_r2, box[2 * g], box[2 * g + 1]))
-                        a |= 1u << g;
+                    a = a && box_accepts(cm, open_r2, box[2 * g], box[2 * g + 1]);
                 return a;
             };
 
@@ -1436,15 +1371,14 @@ namespace nbg
                 const int4 meta = *reinterpret_cast<const int4*>(&nodes[0].open_r2);
                 if (cm.w != 0.f)
                 {
-                    const unsigned a = accepting(cm, __int_as_float(meta.x), all);
-                    const unsigned o = all & ~a;
-                    append(lane == 0 ? a : 0u, cm);
-                    if (o && meta.y < 0)
-                        append_range(meta.z, meta.w, o);
-                    else if (o)
+                    if (accepts(cm, __int_as_float(meta.x)))
+                        append(lane == 0, cm);
+                    else if (meta.y < 0)
+                        append_range(meta.z, meta.w);
+                    else
                     {
                         if (lane == 0)
-                            stk[0] = o << 28;
+                            stk[0] = 0;
                         sp = 1;
                     }
                 }
@@ -1466,22 +1400,17 @@ namespace nbg
                 const int k = min(sp, 4);
                 const int slot = lane >> 3;
                 int c = 0;              // 0: no child (cell 0 is the root, never a child)
-                unsigned open = 0;      // the sub-groups that opened the parent
                 if (slot < k)
-                {
-                    const unsigned e = stk[sp - 1 - slot];
-                    open = e >> 28;
-                    c = nodes[e & 0x0fffffffu].child[lane & 7];
-                }
+                    c = nodes[stk[sp - 1 - slot]].child[lane & 7];
                 __syncwarp();           // every parent read before pushes overwrite its slot
                 sp -= k;
-                unsigned take = 0, push = 0, bucket = 0;
+                bool take = false, push = false, bucket = false;
                 float4 src = make_float4(0.f, 0.f, 0.f, 0.f);
                 int4 meta = make_int4(0, 0, 0, 0);
                 if (c < 0)
                 {
                     src = spm[~c];      // a leaf: always applied (bhtree.cpp:115-116)
-                    take = src.w != 0.f ? open : 0u;
+                    take = src.w != 0.f;
                 }
                 else if (c > 0)
                 {
@@ -1489,33 +1418,34 @@ namespace nbg
                     meta = *reinterpret_cast<const int4*>(&nodes[c].open_r2);
                     if (cm.w != 0.f)    // empty cells are skipped (bhtree.cpp:109-113)
                     {
-                        take = accepting(cm, __int_as_float(meta.x), open);
-                        src = cm;
-                        const unsigned o = open & ~take;
-                        if (o && meta.y < 0)
-                            bucket = o;
+                        if (accepts(cm, __int_as_float(meta.x)))
+                        {
+                            src = cm;
+                            take = true;
+                        }
+                        else if (meta.y < 0)
+                            bucket = true;
                         else
-                            push = o;
+                            push = true;
                     }
                 }
                 append(take, src);
-                const unsigned pm = __ballot_sync(0xffffffffu, push != 0u);
+                const unsigned pm = __ballot_sync(0xffffffffu, push);
                 if (push)
                 {
                     const int at = sp + __popc(pm & lt);
                     if (at < kGroupStack)
-                        stk[at] = static_cast<unsigned>(c) | (push << 28);
+                        stk[at] = c;
                     else
                         atomicOr(err, DEV_ERR_BOUNDS);
                 }
                 sp = min(kGroupStack, sp + __popc(pm));
-                unsigned bm = __ballot_sync(0xffffffffu, bucket != 0u);
+                unsigned bm = __ballot_sync(0xffffffffu, bucket);
                 while (bm)
                 {
                     const int bl = __ffs(bm) - 1;
                     bm &= bm - 1;
-                    append_range(__shfl_sync(0xffffffffu, meta.z, bl), __shfl_sync(0xffffffffu, meta.w, bl),
-                                 __shfl_sync(0xffffffffu, bucket, bl));
+                    append_range(__shfl_sync(0xffffffffu, meta.z, bl), __shfl_sync(0xffffffffu, meta.w, bl));
                 }
                 __syncwarp();
             }
@@ -1745,14 +1675,15 @@ namespace nbg
             // Group walk: 128 targets per group (4 per lane) while the groups outnumber the
             // resident warps, else 64. NBODY_CUDA_BH_GROUP (64, 128 or 256) overrides; the
             // group size changes which cells each target applies, not the bar they meet.
-            if (ni >= (1 << 28))
-                return ctx_fail(ctx, NBODY_ERR_UNSUPPORTED, "the group walk takes fewer than 2^28 bodies");
             const bool soft = p->law == NBODY_LAW_SOFTENED;
             using Walk = void (*)(const OctNode*, const float4*, const float*, const uint64_t*, const uint32_t*, int,
                                   float, float, float4*, float*, unsigned*, unsigned long long*);
-            Walk f64 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 1> : traverse_list_kernel<NBODY_LAW_CUTOFF, 1>;
-            Walk f128 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 2> : traverse_list_kernel<NBODY_LAW_CUTOFF, 2>;
-            Walk f256 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 4> : traverse_list_kernel<NBODY_LAW_CUTOFF, 4>;
+            Walk f64 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 1, kRuns>
+                            : traverse_list_kernel<NBODY_LAW_CUTOFF, 1, kRuns>;
+            Walk f128 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 2, kRuns>
+                             : traverse_list_kernel<NBODY_LAW_CUTOFF, 2, kRuns>;
+            Walk f256 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 4, kRuns>
+                             : traverse_list_kernel<NBODY_LAW_CUTOFF, 4, kRuns>;
             auto per_sm = [&](Walk fn) {
                 int per = 0;
                 if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kListWarps * 32, 0) != cudaSuccess || per < 1)
