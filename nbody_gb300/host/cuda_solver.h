@@ -40,6 +40,7 @@ namespace nbody
         int precision = NBODY_PREC_FP32;    // nbody_precision
         float eps2 = 0.f;                   // softening^2 for NBODY_LAW_SOFTENED
         int tree_box = 0;                   // 0: the reference's root box; 1: fitted
+        int walk = NBODY_WALK_TARGET;       // nbody_walk: the reference's per-target walk, or per group
     };
 
     class CudaSolver final : public Solver
@@ -198,6 +199,7 @@ namespace nbody
             p.law = _config.law;
             p.precision = _config.precision;
             p.tree_box = _config.tree_box;
+            p.walk = _config.walk;
             return p;
         }
 
