@@ -13,11 +13,12 @@
 //      centre comparisons choose (bounds.h:31-38), whose octant bit is set when the
 //      coordinate is below the centre: reference octant = digit ^ 7;
 //   3. radix_sort_pairs over (code, index): stable, so ties keep index order;
-//   4. gather_kernel + cell_sum_kernel: bodies into Morton order, and exact fixed-point
-//      (int64) prefix sums of m and m*x, whose differences give each cell's mass and COM;
+//   4. gather_sum_kernel: bodies into Morton order, and exact fixed-point (int64) prefix
+//      sums of m and m*x, whose differences give each cell's mass and COM, in one pass;
 //   5. karras_kernel: binary radix tree over the sorted codes (Karras 2012), duplicates
 //      separated by index; each internal node's common-prefix length fixes its octree
-//      level floor(prefix / 3) (capped at 21, the last Morton level);
+//      level floor(prefix / 3) (capped at 21, the last Morton level), and the node is
+//      flagged as an octree node here;
 //   6. octree nodes = binary nodes whose level exceeds their parent's (plus the root).
 //      A reference cell whose bodies all sit in one octant (a chain of single-child
 //      cells) has the same centre of mass and mass at every level of the chain, and the
@@ -64,6 +65,13 @@ namespace nbg
         constexpr int kRuns = 4;            // runs (own acceptance boxes) per group
         constexpr int kBboxBlocks = 1024;
         constexpr int kBboxVals = 8;    // min x y z, max x y z, max |m|, max |x|
+        constexpr int kStatsWords = 8;
+        // The Morton sort: radix passes over the top 45 code bits (octree levels 1-15), then
+        // each run of codes that agree on them (a level-15 cell) is put in order by the low 18
+        // bits. A run longer than kMaxRun (not met by a workload of 16.8M disk and halo
+        // bodies, whose longest is 10) instead makes the build finish with a full sort.
+        constexpr int kRunShift = 18;
+        constexpr int kMaxRun = 32;
         constexpr int kMomThreads = 1024;
         constexpr int kMomItems = 4;
         constexpr int kMomTile = kMomThreads * kMomItems;   // bodies per cell-sum tile
@@ -77,7 +85,6 @@ namespace nbg
         float4* spm = nullptr;          // pos_mass in Morton order
         float* srad = nullptr;          // target radius in Morton order
         int2* child = nullptr;          // binary children: >= 0 internal, < 0 ~leaf
-        int* parent = nullptr;
         int2* range = nullptr;          // [first, last] of each internal node
         int* prefix = nullptr;          // common-prefix bits of each internal node
         uint32_t* octflag = nullptr;
@@ -89,7 +96,8 @@ namespace nbg
         BoxParams* box = nullptr;
         float* bbox_part = nullptr;
         unsigned long long* stats = nullptr;   // [0] interactions, [1] node visits, [2] octree nodes,
-                                               // [3] the traversal's tile counter
+                                               // [3] the traversal's tile counter, [4] the Morton
+                                               // sort's full-sort flag (as unsigned)
         const uint32_t* order = nullptr;       // sorted indices of the last build (keys/vals ping-pong)
         const uint64_t* codes = nullptr;
         bool built = false;                    // a tree for built_n bodies is on the device
@@ -109,10 +117,7 @@ namespace nbg
                                                                const int n, float* __restrict__ part)
     {
         float v[kBboxVals] = { INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.f, 0.f };
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        {
-            const float4 p = src[static_cast<size_t>(i) * stride];
-            const float m = stride == 3 ? src[static_cast<size_t>(i) * 3 + 1].w : p.w;
+        auto fold = [&](const float4 p, const float m) {
             const float x[3] = { p.x, p.y, p.z };
 #pragma unroll
             for (int a = 0; a < 3; ++a)
@@ -124,6 +129,29 @@ namespace nbg
             }
             if (isfinite(m))
                 v[6] = fmaxf(v[6], fabsf(m));
+        };
+        const int step = gridDim.x * blockDim.x;
+        int i = blockIdx.x * blockDim.x + threadIdx.x;
+        // four bodies in flight per thread
+        for (; static_cast<long long>(i) + 3 * step < n; i += 4 * step)
+        {
+            float4 p[4];
+            float m[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+            {
+                const size_t k = static_cast<size_t>(i + u * step);
+                p[u] = src[k * stride];
+                m[u] = stride == 3 ? src[k * 3 + 1].w : p[u].w;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                fold(p[u], m[u]);
+        }
+        for (; i < n; i += step)
+        {
+            const float4 p = src[static_cast<size_t>(i) * stride];
+            fold(p, stride == 3 ? src[static_cast<size_t>(i) * 3 + 1].w : p.w);
         }
         __shared__ float red[kBboxVals][256];
 #pragma unroll
@@ -319,30 +347,100 @@ namespace nbg
         return q < 0 ? 0u : (q > 2097151 ? 2097151u : static_cast<uint64_t>(q));
     }
 
-    __global__ void morton_kernel(const float4* __restrict__ src, const int stride, const int n,
-                                  const BoxParams* __restrict__ box, uint64_t* __restrict__ keys,
-                                  uint32_t* __restrict__ vals)
+    constexpr int kMortonItems = 4;     // bodies per thread, all loads issued first
+
+    __global__ void __launch_bounds__(256) morton_kernel(const float4* __restrict__ src, const int stride,
+                                                         const int n, const BoxParams* __restrict__ box,
+                                                         uint64_t* __restrict__ keys, uint32_t* __restrict__ vals)
     {
-        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        const int base = blockIdx.x * (256 * kMortonItems) + threadIdx.x;
+        float4 p[kMortonItems];
+#pragma unroll
+        for (int j = 0; j < kMortonItems; ++j)
+        {
+            const int i = base + j * 256;
+            p[j] = i < n ? src[static_cast<size_t>(i) * stride] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        const BoxParams& b = *box;
+#pragma unroll
+        for (int j = 0; j < kMortonItems; ++j)
+        {
+            const int i = base + j * 256;
+            if (i >= n)
+                break;
+            uint64_t qx, qy, qz;
+            if (b.exact)
+            {
+                qx = quantise_exact(p[j].x, b.cell_exp, b.lo_cells[0]);
+                qy = quantise_exact(p[j].y, b.cell_exp, b.lo_cells[1]);
+                qz = quantise_exact(p[j].z, b.cell_exp, b.lo_cells[2]);
+            }
+            else
+            {
+                qx = quantise(p[j].x, b.lo[0], b.inv_cell);
+                qy = quantise(p[j].y, b.lo[1], b.inv_cell);
+                qz = quantise(p[j].z, b.lo[2], b.inv_cell);
+            }
+            keys[i] = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
+            vals[i] = static_cast<uint32_t>(i);
+        }
+    }
+
+    // After the radix passes over bits [kRunShift, 63), the codes are in order of their top
+    // bits, and the codes of one run (equal top bits) keep index order. The thread at the
+    // start of a run of 2 .. kMaxRun codes puts it in order of the whole code by a stable
+    // insertion sort, so ties keep index order: the result is the order by (code, index).
+    // A longer run sets *full, and the build sorts everything again by all 63 bits. Other
+    // threads read their neighbours' top bits while a run is being reordered: those bits are
+    // the same for every code of the run, so what they see does not depend on the moment.
+    __global__ void __launch_bounds__(256) run_sort_kernel(uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                           const int n, unsigned* __restrict__ full)
+    {
+        const int i = blockIdx.x * 256 + threadIdx.x;
         if (i >= n)
             return;
-        const float4 p = src[static_cast<size_t>(i) * stride];
-        const BoxParams& b = *box;
-        uint64_t qx, qy, qz;
-        if (b.exact)
+        const uint64_t top = keys[i] >> kRunShift;
+        if (i > 0 && (keys[i - 1] >> kRunShift) == top)
+            return;     // not the first code of its run
+        int len = 1;
+        while (i + len < n && len <= kMaxRun && (keys[i + len] >> kRunShift) == top)
+            ++len;
+        if (len == 1)
+            return;
+        if (len > kMaxRun)
         {
-            qx = quantise_exact(p.x, b.cell_exp, b.lo_cells[0]);
-            qy = quantise_exact(p.y, b.cell_exp, b.lo_cells[1]);
-            qz = quantise_exact(p.z, b.cell_exp, b.lo_cells[2]);
+            atomicOr(full, 1u);
+            return;
         }
-        else
+        for (int a = i + 1; a < i + len; ++a)
         {
-            qx = quantise(p.x, b.lo[0], b.inv_cell);
-            qy = quantise(p.y, b.lo[1], b.inv_cell);
-            qz = quantise(p.z, b.lo[2], b.inv_cell);
+            const uint64_t k = keys[a];
+            const uint32_t v = vals[a];
+            int b = a - 1;
+            while (b >= i && keys[b] > k)
+            {
+                keys[b + 1] = keys[b];
+                vals[b + 1] = vals[b];
+                --b;
+            }
+            keys[b + 1] = k;
+            vals[b + 1] = v;
         }
-        keys[i] = spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
-        vals[i] = static_cast<uint32_t>(i);
+    }
+
+    // Copies a full sort's result back into the buffers the build reads, when *run_if is set.
+    __global__ void __launch_bounds__(256) copy_back_kernel(const uint64_t* __restrict__ ks,
+                                                            const uint32_t* __restrict__ vs, uint64_t* __restrict__ kd,
+                                                            uint32_t* __restrict__ vd, const int n,
+                                                            const unsigned* __restrict__ run_if)
+    {
+        if (!*run_if)
+            return;
+        for (int i = blockIdx.x * 256 + threadIdx.x; i < n; i += gridDim.x * 256)
+        {
+            kd[i] = ks[i];
+            vd[i] = vs[i];
+        }
     }
 
     // ------------------------------------------------------------------------------------
@@ -408,91 +506,119 @@ namespace nbg
         return Int64x4{ a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w };
     }
 
-    // Bodies into Morton order (pos_mass, and the radius when srad is given: only the cutoff
-    // law reads it), and the total of each tile's terms.
-    __global__ void __launch_bounds__(kMomThreads) gather_kernel(
-        const float4* __restrict__ src, const int stride, const float4* __restrict__ vel_radius,
-        const uint32_t* __restrict__ order, const int n, const BoxParams* __restrict__ box,
-        float4* __restrict__ spm, float* __restrict__ srad, Int64x4* __restrict__ tile_sum)
+    __device__ __forceinline__ unsigned load_acquire(const unsigned* p)
     {
-        Int64x4 t{ 0, 0, 0, 0 };
-        if (n > 0)
-        {
-            const int mass_shift = box->mass_shift, mom_shift = box->mom_shift;
-            // all of a thread's random reads are issued before any is used (indices past
-            // the end read the last body and are not stored)
-            float4 p[kMomItems];
-            float m[kMomItems], r[kMomItems];
-#pragma unroll
-            for (int j = 0; j < kMomItems; ++j)
-            {
-                const int k = min(blockIdx.x * kMomTile + j * kMomThreads + static_cast<int>(threadIdx.x), n - 1);
-                const uint32_t i = order[k];
-                p[j] = src[static_cast<size_t>(i) * stride];
-                if (stride == 3)
-                {
-                    m[j] = src[static_cast<size_t>(i) * 3 + 1].w;     // Body: {pos, radius}, {vel, mass}
-                    r[j] = p[j].w;
-                }
-                else
-                {
-                    m[j] = p[j].w;
-                    r[j] = vel_radius ? vel_radius[i].w : 0.f;
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < kMomItems; ++j)
-            {
-                const int k = blockIdx.x * kMomTile + j * kMomThreads + threadIdx.x;
-                if (k < n)
-                {
-                    const float4 pm = make_float4(p[j].x, p[j].y, p[j].z, m[j]);
-                    spm[k] = pm;
-                    if (srad)
-                        srad[k] = r[j];
-                    t = add4(t, body_terms(pm, mass_shift, mom_shift));
-                }
-            }
-        }
-        using Op = ScanOps<Int64x4>;
-        for (int d = 16; d > 0; d >>= 1)
-            t = add4(t, Op::shfl_down(t, d));
-        __shared__ Int64x4 warp_sum[kMomThreads / 32];
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        if (lane == 0)
-            warp_sum[warp] = t;
-        __syncthreads();
-        if (warp == 0)
-        {
-            t = warp_sum[lane];
-            for (int d = 16; d > 0; d >>= 1)
-                t = add4(t, Op::shfl_down(t, d));
-            if (lane == 0)
-                tile_sum[blockIdx.x] = t;
-        }
+        unsigned v;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+        return v;
     }
 
-    // psum[k] = the sum of the terms of sorted bodies 0 .. k-1, for k = 0 .. n: each tile
-    // scans its own terms (recomputed from the sorted copy) from its offset, the exclusive
-    // scan of the tile totals.
-    __global__ void __launch_bounds__(kMomThreads) cell_sum_kernel(
-        const float4* __restrict__ spm, const int n, const BoxParams* __restrict__ box,
-        const Int64x4* __restrict__ tile_off, Int64x4* __restrict__ psum)
+    __device__ __forceinline__ void store_release(unsigned* p, const unsigned v)
+    {
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+    }
+
+    __device__ __forceinline__ Int64x4 load_cg(const Int64x4* p)
+    {
+        const longlong2* q = reinterpret_cast<const longlong2*>(p);
+        const longlong2 a = __ldcg(q), b = __ldcg(q + 1);
+        return Int64x4{ a.x, a.y, b.x, b.y };
+    }
+
+    __device__ __forceinline__ Int64x4 shfl_idx4(const Int64x4 v, const int src)
+    {
+        return Int64x4{ __shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+                        __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src) };
+    }
+
+    // Tile states of the single-pass scan: a tile's total published, or the total of it and
+    // every earlier tile.
+    constexpr unsigned kTileAggregate = 1u, kTileInclusive = 2u;
+
+    // Bodies into Morton order (pos_mass, and the radius when srad is given: only the cutoff
+    // law reads it) and psum[k] = the sum of the terms of sorted bodies 0 .. k-1, k = 0 .. n,
+    // in one pass. A CTA takes the next 4096-body tile in launch order (a ticket), gathers it
+    // (four consecutive bodies per thread), scans its terms, publishes its total, and finds
+    // the total of the earlier tiles by decoupled look-back (Merrill & Garland 2016): warp 0
+    // reads 32 earlier tiles' states at a time and sums back to the nearest tile whose
+    // running total is published. Tiles wait only on tiles with earlier tickets, which are
+    // already running, so the wait ends; it is bounded all the same, and a wait that gives
+    // up records DEV_ERR_TIMEOUT. The sums are integers, so the result does not depend on
+    // which tiles published what when.
+    __global__ void __launch_bounds__(kMomThreads) gather_sum_kernel(
+        const float4* __restrict__ src, const int stride, const float4* __restrict__ vel_radius,
+        const uint32_t* __restrict__ order, const int n, const BoxParams* __restrict__ box,
+        float4* __restrict__ spm, float* __restrict__ srad, Int64x4* __restrict__ psum,
+        Int64x4* __restrict__ tile_agg, Int64x4* __restrict__ tile_incl, unsigned* __restrict__ tile_state,
+        unsigned* __restrict__ ticket, unsigned* __restrict__ err)
     {
         using Op = ScanOps<Int64x4>;
+        if (n <= 0)
+            return;
+        __shared__ Int64x4 warp_tot[kMomThreads / 32];
+        __shared__ Int64x4 tile_prefix;
+        __shared__ int tile_s;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (threadIdx.x == 0)
+            tile_s = static_cast<int>(atomicAdd(ticket, 1u));
+        __syncthreads();
+        const int tile = tile_s;
         const int mass_shift = box->mass_shift, mom_shift = box->mom_shift;
-        const int base = blockIdx.x * kMomTile + threadIdx.x * kMomItems;
-        Int64x4 v[kMomItems];
+        const int base = tile * kMomTile + threadIdx.x * kMomItems;
+
+        // gather: every random read is issued before any is used (indices past the end read
+        // the last body and are not stored)
+        uint32_t idx[kMomItems];
+        if (base + kMomItems <= n)
+        {
+            const uint4 o = *reinterpret_cast<const uint4*>(order + base);
+            idx[0] = o.x;
+            idx[1] = o.y;
+            idx[2] = o.z;
+            idx[3] = o.w;
+        }
+        else
+        {
+#pragma unroll
+            for (int k = 0; k < kMomItems; ++k)
+                idx[k] = order[min(base + k, n - 1)];
+        }
+        float4 p[kMomItems];
+        float m[kMomItems], r[kMomItems];
+#pragma unroll
+        for (int k = 0; k < kMomItems; ++k)
+        {
+            const uint32_t i = idx[k];
+            p[k] = src[static_cast<size_t>(i) * stride];
+            if (stride == 3)
+            {
+                m[k] = src[static_cast<size_t>(i) * 3 + 1].w;     // Body: {pos, radius}, {vel, mass}
+                r[k] = p[k].w;
+            }
+            else
+            {
+                m[k] = p[k].w;
+                r[k] = vel_radius ? vel_radius[i].w : 0.f;
+            }
+        }
+        // the thread's total here; its bodies' terms are formed again for the prefixes below
+        // (cheaper than holding four more Int64x4 through the scan)
         Int64x4 run{ 0, 0, 0, 0 };
 #pragma unroll
         for (int k = 0; k < kMomItems; ++k)
         {
             const int i = base + k;
-            const Int64x4 q = i < n ? body_terms(spm[i], mass_shift, mom_shift) : Int64x4{ 0, 0, 0, 0 };
-            v[k] = run;
-            run = add4(run, q);
+            p[k].w = m[k];
+            if (i < n)
+            {
+                spm[i] = p[k];
+                if (srad)
+                    srad[i] = r[k];
+                run = add4(run, body_terms(p[k], mass_shift, mom_shift));
+            }
         }
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+        // the tile's scan: within warps, then over the warps' totals
         Int64x4 incl = run;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1)
@@ -501,13 +627,13 @@ namespace nbg
             if (lane >= d)
                 incl = add4(incl, o);
         }
-        __shared__ Int64x4 warp_tot[kMomThreads / 32];
         if (lane == 31)
             warp_tot[warp] = incl;
         __syncthreads();
         if (warp == 0)
         {
-            Int64x4 wi = warp_tot[lane];
+            constexpr int kWarpsPerTile = kMomThreads / 32;
+            Int64x4 wi = lane < kWarpsPerTile ? warp_tot[lane] : Int64x4{ 0, 0, 0, 0 };
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1)
             {
@@ -515,13 +641,71 @@ namespace nbg
                 if (lane >= d)
                     wi = add4(wi, o);
             }
-            warp_tot[lane] = wi;    // inclusive over warps
+            if (lane < kWarpsPerTile)
+                warp_tot[lane] = wi;    // inclusive over warps
+            const Int64x4 agg = shfl_idx4(wi, 31);      // the tile's total
+            // publish the tile's own total at once: later tiles may be waiting for it
+            if (lane == 0)
+            {
+                if (tile == 0)
+                    tile_incl[0] = agg;
+                else
+                    tile_agg[tile] = agg;
+                __threadfence();
+                store_release(&tile_state[tile], tile == 0 ? kTileInclusive : kTileAggregate);
+            }
+            Int64x4 before{ 0, 0, 0, 0 };
+            int j = tile - 1;           // the latest tile not yet summed
+            uint64_t t0 = 0;
+            while (j >= 0)
+            {
+                const int jj = j - lane;
+                const unsigned st = jj >= 0 ? load_acquire(&tile_state[jj]) : kTileInclusive;
+                const unsigned incl_mask = __ballot_sync(0xffffffffu, st == kTileInclusive);
+                const unsigned none_mask = __ballot_sync(0xffffffffu, st == 0u);
+                // lanes up to and including the first inclusive one are the ones summed
+                const int first = incl_mask ? __ffs(incl_mask) - 1 : 31;
+                const unsigned need = first == 31 ? 0xffffffffu : (2u << first) - 1u;
+                if (none_mask & need)
+                {
+                    if (!t0)
+                        t0 = globaltimer();
+                    else if (globaltimer() - t0 > kWaitLimitNs)
+                    {
+                        if (lane == 0)
+                            atomicOr(err, DEV_ERR_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(64);
+                    continue;
+                }
+                Int64x4 val{ 0, 0, 0, 0 };
+                if (lane <= first && jj >= 0)
+                    val = load_cg(st == kTileInclusive ? &tile_incl[jj] : &tile_agg[jj]);
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1)
+                    val = add4(val, Op::shfl_down(val, d));
+                before = add4(before, shfl_idx4(val, 0));     // lane 0 holds the sum
+                if (incl_mask)
+                    break;
+                j -= 32;
+            }
+            if (lane == 0)
+            {
+                if (tile > 0)
+                {
+                    tile_incl[tile] = add4(before, agg);
+                    __threadfence();
+                    store_release(&tile_state[tile], kTileInclusive);
+                }
+                tile_prefix = before;
+            }
         }
         __syncthreads();
         Int64x4 excl = Op::shfl_up(incl, 1);
         if (lane == 0)
             excl = Int64x4{ 0, 0, 0, 0 };
-        Int64x4 off = add4(tile_off[blockIdx.x], excl);
+        Int64x4 off = add4(tile_prefix, excl);
         if (warp > 0)
             off = add4(off, warp_tot[warp - 1]);
 #pragma unroll
@@ -529,46 +713,92 @@ namespace nbg
         {
             const int i = base + k;
             if (i < n)
-                psum[i] = add4(off, v[k]);
+            {
+                psum[i] = off;
+                off = add4(off, body_terms(p[k], mass_shift, mom_shift));
+            }
         }
         if (base <= n - 1 && n - 1 < base + kMomItems)
-            psum[n] = add4(off, run);
+            psum[n] = off;
     }
 
     // ------------------------------------------------------------------------------------
     // 5. binary radix tree (Karras 2012)
     // ------------------------------------------------------------------------------------
-    __device__ __forceinline__ int delta(const uint64_t* __restrict__ keys, const int n, const int i, const int j)
-    {
-        if (j < 0 || j >= n)
-            return -1;
-        const uint64_t a = keys[i], b = keys[j];
-        if (a != b)
-            return __clzll(static_cast<long long>(a ^ b));
-        return 64 + __clz(static_cast<int>(static_cast<unsigned>(i) ^ static_cast<unsigned>(j)));
-    }
+    constexpr int kKarrasThreads = 256;
+    constexpr int kKarrasHalo = 256;        // keys staged on either side of a block's nodes
+    constexpr int kKarrasWin = kKarrasThreads + 2 * kKarrasHalo;
 
-    __global__ void karras_kernel(const uint64_t* __restrict__ keys, const int n, int2* __restrict__ child,
-                                  int* __restrict__ parent, int2* __restrict__ range, int* __restrict__ prefix)
+    // The sorted keys around one block's nodes, staged in shared memory: the searches of most
+    // nodes stay within kKarrasHalo keys of the node, and read there instead of through the
+    // cache hierarchy; a probe outside the window reads global memory.
+    struct KeyWindow
     {
-        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        const uint64_t* __restrict__ keys;
+        const uint64_t* win;
+        int w0;         // key index of win[0]
+        int n;
+
+        __device__ __forceinline__ uint64_t at(const int k) const
+        {
+            const unsigned t = static_cast<unsigned>(k - w0);
+            return t < static_cast<unsigned>(kKarrasWin) ? win[t] : keys[k];
+        }
+
+        // common-prefix length of keys i and j (0 <= i < n), duplicates separated by index;
+        // -1 for j outside [0, n)
+        __device__ __forceinline__ int delta(const uint64_t a, const int i, const int j) const
+        {
+            if (j < 0 || j >= n)
+                return -1;
+            const uint64_t b = at(j);
+            if (a != b)
+                return __clzll(static_cast<long long>(a ^ b));
+            return 64 + __clz(static_cast<int>(static_cast<unsigned>(i) ^ static_cast<unsigned>(j)));
+        }
+    };
+
+    __device__ __forceinline__ int level_of(const int prefix) { return min(kMaxLevel, prefix / 3); }
+
+    // Node i of the binary radix tree, and whether it is an octree node. A node's range
+    // [lo, hi] is bounded by two splits, delta(lo - 1, lo) and delta(hi, hi + 1), both below
+    // its own; its parent splits at the larger of the two (the smallest range that strictly
+    // contains [lo, hi] ends where the shared prefix first shortens), so the parent's
+    // prefix is known here without a parent array. A node is an octree node when its level
+    // exceeds its parent's, or it is the root.
+    __global__ void __launch_bounds__(kKarrasThreads) karras_kernel(
+        const uint64_t* __restrict__ keys, const int n, int2* __restrict__ child, int2* __restrict__ range,
+        int* __restrict__ prefix, uint32_t* __restrict__ flag)
+    {
+        __shared__ uint64_t win[kKarrasWin];
+        const int w0 = static_cast<int>(blockIdx.x) * kKarrasThreads - kKarrasHalo;
+        for (int t = threadIdx.x; t < kKarrasWin; t += kKarrasThreads)
+        {
+            const int k = w0 + t;
+            if (k >= 0 && k < n)
+                win[t] = keys[k];
+        }
+        __syncthreads();
+        const KeyWindow kw{ keys, win, w0, n };
+        const int i = blockIdx.x * kKarrasThreads + threadIdx.x;
         if (i >= n - 1)
             return;
-        const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
-        const int dmin = delta(keys, n, i, i - d);
+        const uint64_t ki = win[i - w0];
+        const int d = (kw.delta(ki, i, i + 1) - kw.delta(ki, i, i - 1)) >= 0 ? 1 : -1;
+        const int dmin = kw.delta(ki, i, i - d);
         int lmax = 2;
-        while (delta(keys, n, i, i + lmax * d) > dmin)
+        while (kw.delta(ki, i, i + lmax * d) > dmin)
             lmax <<= 1;
         int l = 0;
         for (int t = lmax >> 1; t >= 1; t >>= 1)
-            if (delta(keys, n, i, i + (l + t) * d) > dmin)
+            if (kw.delta(ki, i, i + (l + t) * d) > dmin)
                 l += t;
         const int j = i + l * d;
-        const int dnode = delta(keys, n, i, j);
+        const int dnode = kw.delta(ki, i, j);
         int s = 0;
         for (int t = (l + 1) >> 1;; t = (t + 1) >> 1)
         {
-            if (delta(keys, n, i, i + (s + t) * d) > dnode)
+            if (kw.delta(ki, i, i + (s + t) * d) > dnode)
                 s += t;
             if (t == 1)
                 break;
@@ -579,25 +809,12 @@ namespace nbg
         const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
         child[i] = make_int2(left, right);
         range[i] = make_int2(lo, hi);
-        prefix[i] = dnode - 1;     // codes are 63-bit: the top key bit is always shared
-        if (left >= 0)
-            parent[left] = i;
-        if (right >= 0)
-            parent[right] = i;
-        if (i == 0)
-            parent[0] = -1;
-    }
-
-    __device__ __forceinline__ int level_of(const int prefix) { return min(kMaxLevel, prefix / 3); }
-
-    __global__ void octflag_kernel(const int* __restrict__ parent, const int* __restrict__ prefix, const int m,
-                                   uint32_t* __restrict__ flag)
-    {
-        const int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i >= m)
-            return;
-        const int p = parent[i];
-        flag[i] = (i == 0 || p < 0 || level_of(prefix[i]) > level_of(prefix[p])) ? 1u : 0u;
+        const int pre = dnode - 1;      // codes are 63-bit: the top key bit is always shared
+        prefix[i] = pre;
+        // the bound at i's end of the range is delta(i, i - d), already known as dmin; the
+        // bound at j's end is delta(j, j + d) (-1 past either end of the array)
+        const int up = max(dmin, kw.delta(kw.at(j), j, j + d)) - 1;
+        flag[i] = (i == 0 || level_of(pre) > level_of(up)) ? 1u : 0u;
     }
 
     // ------------------------------------------------------------------------------------
@@ -606,19 +823,26 @@ namespace nbg
     // The children of a cell: walking down through the binary nodes of the cell's own level
     // (at most three splits below it), every leaf body and every node of a deeper level is
     // one child. Right subtrees first, which is the order the traversal has always used.
+    // Children are kept in registers (kid[k] selected by a static index) and stored at once.
+    __device__ __forceinline__ void emit_child(int (&kid)[8], int& nc, const int v, unsigned* __restrict__ err)
+    {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            kid[k] = k == nc ? v : kid[k];
+        if (nc >= 8)
+            atomicOr(err, DEV_ERR_BOUNDS);
+        ++nc;
+    }
+
     template <int DEPTH>
     __device__ __forceinline__ void collect_children(const int c, const int2* __restrict__ child,
                                                      const uint32_t* __restrict__ flag,
-                                                     const uint32_t* __restrict__ octidx, int* __restrict__ out,
+                                                     const uint32_t* __restrict__ octidx, int (&kid)[8],
                                                      int& nc, unsigned* __restrict__ err)
     {
         if (c < 0 || flag[c])
         {
-            if (nc < 8)
-                out[nc] = c < 0 ? c : static_cast<int>(octidx[c]);
-            else
-                atomicOr(err, DEV_ERR_BOUNDS);
-            ++nc;
+            emit_child(kid, nc, c < 0 ? c : static_cast<int>(octidx[c]), err);
             return;
         }
         if (DEPTH == 0)
@@ -627,8 +851,26 @@ namespace nbg
             return;
         }
         const int2 ch = child[c];
-        collect_children<DEPTH ? DEPTH - 1 : 0>(ch.y, child, flag, octidx, out, nc, err);
-        collect_children<DEPTH ? DEPTH - 1 : 0>(ch.x, child, flag, octidx, out, nc, err);
+        collect_children<DEPTH ? DEPTH - 1 : 0>(ch.y, child, flag, octidx, kid, nc, err);
+        collect_children<DEPTH ? DEPTH - 1 : 0>(ch.x, child, flag, octidx, kid, nc, err);
+    }
+
+    // position of the r-th set bit (from 0) of v, for r < popc(v)
+    __device__ __forceinline__ int select_bit(unsigned v, int r)
+    {
+        int pos = 0;
+#pragma unroll
+        for (int w = 16; w > 0; w >>= 1)
+        {
+            const int c = __popc(v & ((1u << w) - 1u));
+            if (r >= c)
+            {
+                r -= c;
+                v >>= w;
+                pos += w;
+            }
+        }
+        return pos;
     }
 
     // An int64 as float: |v| split into two 32-bit halves, each converted exactly or with one
@@ -642,56 +884,88 @@ namespace nbg
         return v < 0 ? -f : f;
     }
 
-    // latency bound (chains of dependent loads): full occupancy, 32 registers
-    __global__ void __launch_bounds__(256, 7) octnode_kernel(const int2* __restrict__ child, const int2* __restrict__ range,
+    constexpr int kOctSpan = 4;     // binary nodes per lane that one warp scans for octree nodes
+
+    // One octree record per flagged binary node. Latency bound (chains of dependent loads),
+    // so a warp first gathers the flagged nodes among 32 * kOctSpan consecutive binary nodes
+    // (ballots; about 40 % are flagged) and its lanes then take them in turn, instead of
+    // idling on unflagged ones.
+    __global__ void __launch_bounds__(256) octnode_kernel(const int2* __restrict__ child, const int2* __restrict__ range,
                                    const int* __restrict__ prefix, const uint32_t* __restrict__ flag,
                                    const uint32_t* __restrict__ octidx, const Int64x4* __restrict__ psum,
                                    const int m, const BoxParams* __restrict__ box, const float theta,
                                    OctNode* __restrict__ nodes, unsigned* __restrict__ err,
                                    unsigned long long* __restrict__ stats)
     {
-        const int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i == 0)
+        const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+        if (gt == 0)
             atomicAdd(&stats[2], static_cast<unsigned long long>(octidx[m - 1] + flag[m - 1]));
-        if (i >= m || !flag[i])
-            return;
-        const int2 rg = range[i];
-        const int pre = prefix[i];
-        const int lvl = level_of(pre);
-        const Int64x4 hi = psum[rg.y + 1], lo = psum[rg.x];
-        const long long ms = hi.w - lo.w;   // exact: the cell's own terms
-        OctNode* out = nodes + octidx[i];
-        if (ms > 0)
+        const int lane = threadIdx.x & 31;
+        const int first = (gt >> 5) * (32 * kOctSpan);
+        if (first >= m)
+            return;     // the whole warp
+        unsigned mask[kOctSpan];
+        int total = 0;
+#pragma unroll
+        for (int u = 0; u < kOctSpan; ++u)
         {
-            // com = (sum of m x 2^mom_shift) / (sum of m 2^mass_shift) * 2^(mass_shift - mom_shift),
-            // in float: the quotient lies in [-1, 1] before the exact power-of-two scaling
-            const int shift = box->mass_shift - box->mom_shift;
-            const float fm = i64_to_float(ms);
-            const float rm = __frcp_rn(fm);
-            out->com_mass = make_float4(ldexpf(i64_to_float(hi.x - lo.x) * rm, shift),
-                                        ldexpf(i64_to_float(hi.y - lo.y) * rm, shift),
-                                        ldexpf(i64_to_float(hi.z - lo.z) * rm, shift),
-                                        ldexpf(fm, -box->mass_shift));
+            const int i = first + u * 32 + lane;
+            mask[u] = __ballot_sync(0xffffffffu, i < m && flag[i] != 0u);
+            total += __popc(mask[u]);
         }
-        else
-            out->com_mass = make_float4(0.f, 0.f, 0.f, 0.f);
-        // the reference's node size is the root size halved per level, in float
-        const float sz = ldexpf(box->edge_f, -lvl);
-        const float open_r2 = __fmul_rn(__fmul_rn(sz, sz), __fmul_rn(theta, theta));
-        int4* kids = reinterpret_cast<int4*>(out->child);
-        kids[0] = make_int4(0, 0, 0, 0);
-        kids[1] = make_int4(0, 0, 0, 0);
-        int nc = 0;
-        if (pre >= 3 * kMaxLevel)
-            nc = -1;     // bucket: identical codes, bodies applied one by one
-        else
+        const int shift = box->mass_shift - box->mom_shift;
+        for (int q = lane; q < total; q += 32)
         {
-            const int2 ch = child[i];
-            collect_children<2>(ch.y, child, flag, octidx, out->child, nc, err);
-            collect_children<2>(ch.x, child, flag, octidx, out->child, nc, err);
-            nc = min(nc, 8);
+            int u = 0, r = q;
+#pragma unroll
+            for (int k = 0; k < kOctSpan - 1; ++k)
+                if (u == k && r >= __popc(mask[k]))
+                {
+                    r -= __popc(mask[k]);
+                    u = k + 1;
+                }
+            unsigned mu = mask[0];
+#pragma unroll
+            for (int k = 1; k < kOctSpan; ++k)
+                mu = u == k ? mask[k] : mu;
+            const int i = first + u * 32 + select_bit(mu, r);
+            const int2 rg = range[i];
+            const int pre = prefix[i];
+            const int lvl = level_of(pre);
+            const Int64x4 hi = psum[rg.y + 1], lo = psum[rg.x];
+            const long long ms = hi.w - lo.w;   // exact: the cell's own terms
+            OctNode* out = nodes + octidx[i];
+            float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (ms > 0)
+            {
+                // com = (sum of m x 2^mom_shift) / (sum of m 2^mass_shift) * 2^(mass_shift - mom_shift),
+                // in float: the quotient lies in [-1, 1] before the exact power-of-two scaling
+                const float fm = i64_to_float(ms);
+                const float rm = __frcp_rn(fm);
+                cm = make_float4(ldexpf(i64_to_float(hi.x - lo.x) * rm, shift),
+                                 ldexpf(i64_to_float(hi.y - lo.y) * rm, shift),
+                                 ldexpf(i64_to_float(hi.z - lo.z) * rm, shift), ldexpf(fm, -box->mass_shift));
+            }
+            // the reference's node size is the root size halved per level, in float
+            const float sz = ldexpf(box->edge_f, -lvl);
+            const float open_r2 = __fmul_rn(__fmul_rn(sz, sz), __fmul_rn(theta, theta));
+            int kid[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+            int nc = 0;
+            if (pre >= 3 * kMaxLevel)
+                nc = -1;     // bucket: identical codes, bodies applied one by one
+            else
+            {
+                const int2 ch = child[i];
+                collect_children<2>(ch.y, child, flag, octidx, kid, nc, err);
+                collect_children<2>(ch.x, child, flag, octidx, kid, nc, err);
+                nc = min(nc, 8);
+            }
+            out->com_mass = cm;
+            *reinterpret_cast<int4*>(&out->open_r2) = make_int4(__float_as_int(open_r2), nc, rg.x, rg.y);
+            int4* kids = reinterpret_cast<int4*>(out->child);
+            kids[0] = make_int4(kid[0], kid[1], kid[2], kid[3]);
+            kids[1] = make_int4(kid[4], kid[5], kid[6], kid[7]);
         }
-        *reinterpret_cast<int4*>(&out->open_r2) = make_int4(__float_as_int(open_r2), nc, rg.x, rg.y);
     }
 
     // ------------------------------------------------------------------------------------
@@ -1505,7 +1779,7 @@ namespace nbg
                     e = cudaMallocAsync(reinterpret_cast<void**>(&b.bbox_part), kBboxBlocks * kBboxVals * sizeof(float),
                                         ctx->stream);
                 if (e == cudaSuccess)
-                    e = cudaMallocAsync(reinterpret_cast<void**>(&b.stats), 4 * sizeof(unsigned long long), ctx->stream);
+                    e = cudaMallocAsync(reinterpret_cast<void**>(&b.stats), kStatsWords * sizeof(unsigned long long), ctx->stream);
                 if (e != cudaSuccess)
                     return ctx_cuda_fail(ctx, e, "tree allocation");
             }
@@ -1515,7 +1789,11 @@ namespace nbg
                 return st;
             const size_t cap = std::max(n, b.cap + b.cap / 2);
             const size_t tiles = (cap + kMomTile - 1) / kMomTile;
-            const size_t tb = std::max(sort_temp_bytes(cap), (tiles + scan_temp_elems(tiles)) * sizeof(Int64x4));
+            // the sort's temporaries; the cell sums' tile totals, running totals, states and
+            // ticket; the octree compaction's scan
+            const size_t tb = std::max(sort_temp_bytes(cap),
+                                       std::max(2 * tiles * sizeof(Int64x4) + (tiles + 1) * sizeof(unsigned),
+                                                scan_temp_elems(cap) * sizeof(uint32_t)));
             cudaError_t e = cudaSuccess;
             cudaStream_t s = ctx->stream;
             for (int k = 0; k < 2 && e == cudaSuccess; ++k)
@@ -1527,7 +1805,6 @@ namespace nbg
             if (e == cudaSuccess) e = grow(&b.spm, cap, s);
             if (e == cudaSuccess) e = grow(&b.srad, cap, s);
             if (e == cudaSuccess) e = grow(&b.child, cap, s);
-            if (e == cudaSuccess) e = grow(&b.parent, cap, s);
             if (e == cudaSuccess) e = grow(&b.range, cap, s);
             if (e == cudaSuccess) e = grow(&b.prefix, cap, s);
             if (e == cudaSuccess) e = grow(&b.octflag, cap, s);
@@ -1573,10 +1850,9 @@ namespace nbg
         int stride = 1;
         const float4* src = body_src(ctx, &stride);
         const int ni = static_cast<int>(n);
-        const unsigned blocks = ceil_div(n, 256);
         uint64_t& L = ctx->launches;
 
-        if (const cudaError_t me = cudaMemsetAsync(b.stats, 0, 4 * sizeof(unsigned long long), s))
+        if (const cudaError_t me = cudaMemsetAsync(b.stats, 0, kStatsWords * sizeof(unsigned long long), s))
             return ctx_cuda_fail(ctx, me, "tree statistics");
         // tree_box = 0 is the reference's fixed root box; it needs a positive size
         const bool auto_box = p->tree_box != 0 || !(p->size > 0.f);
@@ -1585,28 +1861,51 @@ namespace nbg
         ++L;
         box_final_kernel<<<1, 256, 0, s>>>(b.bbox_part, kBboxBlocks, ni, auto_box ? 1 : 0, p->size, b.box);
         ++L;
-        morton_kernel<<<blocks, 256, 0, s>>>(src, stride, ni, b.box, b.keys[0], b.vals[0]);
+        morton_kernel<<<ceil_div(n, 256 * kMortonItems), 256, 0, s>>>(src, stride, ni, b.box, b.keys[0], b.vals[0]);
         ++L;
         bool in_alt = false;
-        cudaError_t e = radix_sort_pairs(b.keys[0], b.vals[0], b.keys[1], b.vals[1], n, 0, 63, b.temp, s, &L, &in_alt,
-                                         ctx->dev_error);
+        cudaError_t e = radix_sort_pairs(b.keys[0], b.vals[0], b.keys[1], b.vals[1], n, kRunShift, 63, b.temp, s, &L,
+                                         &in_alt, ctx->dev_error);
         if (e != cudaSuccess)
             return ctx_cuda_fail(ctx, e, "radix sort");
+        if (n > 1)
+        {
+            // runs of equal top bits into order; a run too long for that sorts everything
+            // again by all bits, from the current order (its ties are in index order too), and
+            // copies the result back, so that the sorted pairs are where the passes left them
+            const int cur = in_alt ? 1 : 0;
+            unsigned* full = reinterpret_cast<unsigned*>(b.stats + 4);
+            run_sort_kernel<<<ceil_div(n, 256), 256, 0, s>>>(b.keys[cur], b.vals[cur], ni, full);
+            ++L;
+            bool alt2 = false;
+            e = radix_sort_pairs(b.keys[cur], b.vals[cur], b.keys[1 - cur], b.vals[1 - cur], n, 0, 63, b.temp, s, &L,
+                                 &alt2, ctx->dev_error, full, (63 - kRunShift + 8) / 9);
+            if (e != cudaSuccess)
+                return ctx_cuda_fail(ctx, e, "radix sort");
+            if (alt2)
+            {
+                copy_back_kernel<<<1024, 256, 0, s>>>(b.keys[1 - cur], b.vals[1 - cur], b.keys[cur], b.vals[cur], ni,
+                                                         full);
+                ++L;
+            }
+        }
         const uint64_t* keys = b.keys[in_alt ? 1 : 0];
         const uint32_t* order = b.vals[in_alt ? 1 : 0];
         b.order = order;
         b.codes = keys;
         const unsigned tiles = std::max(1u, ceil_div(n, kMomTile));
-        Int64x4* tile_sum = static_cast<Int64x4*>(b.temp);
-        const bool radius = p->law == NBODY_LAW_CUTOFF;
-        gather_kernel<<<tiles, kMomThreads, 0, s>>>(src, stride,
-                                                    radius && ctx->layout != NBODY_LAYOUT_AOS ? ctx->vr : nullptr,
-                                                    order, ni, b.box, b.spm, radius ? b.srad : nullptr, tile_sum);
-        ++L;
-        e = exclusive_scan<Int64x4>(tile_sum, tile_sum, tiles, tile_sum + tiles, s, &L);
+        Int64x4* tile_agg = static_cast<Int64x4*>(b.temp);
+        Int64x4* tile_incl = tile_agg + tiles;
+        unsigned* tile_state = reinterpret_cast<unsigned*>(tile_incl + tiles);      // + the ticket
+        e = cudaMemsetAsync(tile_state, 0, (tiles + 1) * sizeof(unsigned), s);
         if (e != cudaSuccess)
             return ctx_cuda_fail(ctx, e, "cell sums");
-        cell_sum_kernel<<<tiles, kMomThreads, 0, s>>>(b.spm, ni, b.box, tile_sum, b.psum);
+        const bool radius = p->law == NBODY_LAW_CUTOFF;
+        gather_sum_kernel<<<tiles, kMomThreads, 0, s>>>(src, stride,
+                                                        radius && ctx->layout != NBODY_LAYOUT_AOS ? ctx->vr : nullptr,
+                                                        order, ni, b.box, b.spm, radius ? b.srad : nullptr, b.psum,
+                                                        tile_agg, tile_incl, tile_state, tile_state + tiles,
+                                                        ctx->dev_error);
         ++L;
         if (n < 2)
         {
@@ -1616,14 +1915,13 @@ namespace nbg
             return NBODY_OK;
         }
         const int m = ni - 1;
-        karras_kernel<<<ceil_div(m, 256), 256, 0, s>>>(keys, ni, b.child, b.parent, b.range, b.prefix);
-        ++L;
-        octflag_kernel<<<ceil_div(m, 256), 256, 0, s>>>(b.parent, b.prefix, m, b.octflag);
+        karras_kernel<<<ceil_div(m, kKarrasThreads), kKarrasThreads, 0, s>>>(keys, ni, b.child, b.range, b.prefix,
+                                                                            b.octflag);
         ++L;
         e = exclusive_scan<uint32_t>(b.octflag, b.octidx, m, static_cast<uint32_t*>(b.temp), s, &L);
         if (e != cudaSuccess)
             return ctx_cuda_fail(ctx, e, "octree compaction");
-        octnode_kernel<<<ceil_div(m, 256), 256, 0, s>>>(b.child, b.range, b.prefix, b.octflag, b.octidx, b.psum, m, b.box,
+        octnode_kernel<<<ceil_div(m, 256 * kOctSpan), 256, 0, s>>>(b.child, b.range, b.prefix, b.octflag, b.octidx, b.psum, m, b.box,
                                                          p->theta, b.nodes, ctx->dev_error, b.stats);
         ++L;
         e = cudaGetLastError();
@@ -1801,7 +2099,7 @@ namespace nbg
             cudaFree(b.keys[k]);
             cudaFree(b.vals[k]);
         }
-        void* ptrs[] = { b.spm, b.srad, b.child, b.parent, b.range, b.prefix, b.octflag, b.octidx, b.psum,
+        void* ptrs[] = { b.spm, b.srad, b.child, b.range, b.prefix, b.octflag, b.octidx, b.psum,
                          b.nodes, b.temp, b.box, b.bbox_part, b.stats };
         for (void* q : ptrs)
             cudaFree(q);

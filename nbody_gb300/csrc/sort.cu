@@ -37,7 +37,7 @@ namespace nbg
         constexpr int kDigits = 1 << kBits;
         constexpr unsigned kMask = kDigits - 1;
         constexpr int kPer = kDigits / kThreads;      // digits per thread in the per-digit steps
-        constexpr int kMaxPasses = 8;
+        constexpr int kMaxPasses = 16;      // over the calls that share one set of temporaries
         constexpr int kHistThreads = 1024;
 
         // A tile's published count for one digit: flag in bits 62-63, the pass's epoch
@@ -79,8 +79,11 @@ namespace nbg
     // Histograms of the digits of all passes, in one read of the keys.
     __global__ void __launch_bounds__(kHistThreads) digit_hist_kernel(const uint64_t* __restrict__ keys, const int n,
                                                                       const int shift0, const int passes,
-                                                                      uint32_t* __restrict__ ghist)
+                                                                      uint32_t* __restrict__ ghist,
+                                                                      const unsigned* __restrict__ run_if)
     {
+        if (run_if && !*run_if)
+            return;
         __shared__ uint32_t hist[kMaxPasses * kDigits];
         for (int d = threadIdx.x; d < passes * kDigits; d += kHistThreads)
             hist[d] = 0;
@@ -158,8 +161,10 @@ namespace nbg
         const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint64_t* __restrict__ keys_out,
         uint32_t* __restrict__ vals_out, const int n, const int shift, const int pass,
         const uint32_t* __restrict__ ghist, uint64_t* __restrict__ status, uint32_t* __restrict__ ticket,
-        unsigned* __restrict__ err)
+        unsigned* __restrict__ err, const unsigned* __restrict__ run_if)
     {
+        if (run_if && !*run_if)
+            return;
         extern __shared__ __align__(16) unsigned char smem[];
         uint64_t* stage_k = reinterpret_cast<uint64_t*>(smem);                     // kTile
         uint32_t* stage_v = reinterpret_cast<uint32_t*>(stage_k + kTile);          // kTile
@@ -346,7 +351,8 @@ namespace nbg
 
     cudaError_t radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt,
                                  const size_t n, const int begin_bit, const int end_bit, void* temp,
-                                 cudaStream_t stream, uint64_t* launches, bool* in_alt, unsigned* err)
+                                 cudaStream_t stream, uint64_t* launches, bool* in_alt, unsigned* err,
+                                 const unsigned* run_if, const int pass_base)
     {
         *in_alt = false;
         if (n <= 1)
@@ -354,7 +360,7 @@ namespace nbg
         if (n > 0x7fffffffu)
             return cudaErrorInvalidValue;
         const int passes = (end_bit - begin_bit + kBits - 1) / kBits;
-        if (passes < 1 || passes > kMaxPasses)
+        if (passes < 1 || pass_base < 0 || pass_base + passes > kMaxPasses)
             return cudaErrorInvalidValue;
         static const cudaError_t attr = cudaFuncSetAttribute(
             digit_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kPassSmem));
@@ -362,14 +368,18 @@ namespace nbg
             return attr;
         const int tiles = static_cast<int>((n + kTile - 1) / kTile);
         const TempLayout t = layout(temp, static_cast<size_t>(tiles));
-        cudaError_t e = cudaMemsetAsync(temp, 0, t.zero_bytes, stream);
+        // the first call zeroes the tickets, histograms and published counts of every pass;
+        // a later call's passes have their own tickets and histograms, and their counts carry
+        // other epochs
+        cudaError_t e = pass_base == 0 ? cudaMemsetAsync(temp, 0, t.zero_bytes, stream) : cudaSuccess;
         if (e != cudaSuccess)
             return e;
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int hist_grid = std::max(1, std::min((static_cast<int>(n) + kHistThreads - 1) / kHistThreads, 2 * sms));
-        digit_hist_kernel<<<hist_grid, kHistThreads, 0, stream>>>(keys, static_cast<int>(n), begin_bit, passes, t.ghist);
+        digit_hist_kernel<<<hist_grid, kHistThreads, 0, stream>>>(keys, static_cast<int>(n), begin_bit, passes,
+                                                                  t.ghist + pass_base * kDigits, run_if);
         ++*launches;
         e = cudaGetLastError();
         if (e != cudaSuccess)
@@ -380,9 +390,10 @@ namespace nbg
         uint32_t* vout = vals_alt;
         for (int p = 0; p < passes; ++p)
         {
+            const int q = pass_base + p;
             digit_pass_kernel<<<tiles, kThreads, kPassSmem, stream>>>(kin, vin, kout, vout, static_cast<int>(n),
-                                                                       begin_bit + p * kBits, p, t.ghist + p * kDigits,
-                                                                       t.status, t.tickets + p, err);
+                                                                       begin_bit + p * kBits, q, t.ghist + q * kDigits,
+                                                                       t.status, t.tickets + q, err, run_if);
             ++*launches;
             e = cudaGetLastError();
             if (e != cudaSuccess)

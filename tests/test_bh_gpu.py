@@ -109,6 +109,39 @@ def test_sort_order_at_tile_edges(gpu, n):
     assert np.array_equal(codes, ref_codes[ref_order])
 
 
+@pytest.mark.parametrize("max_run", [32, 33])
+def test_sort_order_with_runs_in_one_fine_cell(gpu, max_run):
+    """The Morton sort orders the top 45 code bits by radix passes and then each run of
+    codes that agree on them by the low 18 bits; a run longer than 32 sorts everything again
+    by all bits. Clusters of 2 .. max_run bodies inside one level-15 cell (codes that differ
+    only in their low bits, some identical) take the first path at 32 and the second at 33."""
+    rng = np.random.default_rng(max_run)
+    sizes = rng.integers(2, max_run + 1, 3000)
+    sizes[0] = max_run
+    n = int(sizes.sum()) + 2
+    b = np.zeros((n, 12), np.float32)
+    b[:, 7] = 1.0
+    b[0, :3], b[1, :3] = -30.0, 30.0         # fitted box: edge 64, corner -32 on every axis
+    cell = 64.0 / 2 ** 15                    # level 15
+    k = 2
+    for s in sizes:
+        c = -32.0 + (rng.integers(2 ** 10, 2 ** 15 - 2 ** 10, 3) + 0.5) * cell
+        b[k:k + s, :3] = (c + rng.uniform(-0.45, 0.45, (s, 3)) * cell).astype(np.float32)
+        b[k + s - 1, :3] = b[k, :3]          # one identical pair per cluster
+        k += s
+    b = b[rng.permutation(n)]                # clusters spread over the index range
+    with gpu.Context() as ctx:
+        ctx.upload_bodies(b)
+        codes, order, box = ctx.morton(gpu.params(mode=gpu.MODE_NLOGN, size=0.0, tree_box=1))
+    assert list(box) == [-32.0, -32.0, -32.0, 64.0]
+    ref_codes = O.morton63(b[:, :3], box[:3], 2.0 ** 21 / box[3])
+    ref_order = O.sort_order(ref_codes)
+    runs = np.diff(np.flatnonzero(np.r_[True, np.diff(ref_codes[ref_order] >> np.uint64(18)) != 0, True]))
+    assert runs.max() == max_run
+    assert np.array_equal(order, ref_order)
+    assert np.array_equal(codes, ref_codes[ref_order])
+
+
 def test_sort_order_at_16m(gpu):
     """The sort of the 16.8M disk + halo codes: 4096 tiles per pass, most of them waiting on
     their predecessors' counts, against the oracle's stable order."""
