@@ -157,6 +157,9 @@ namespace nbg
         }
     }
 
+    // PERSIST: a CTA takes tiles until none is left (launched with one CTA per resident slot);
+    // otherwise one tile per CTA (launched with one CTA per tile)
+    template <bool PERSIST>
     __global__ void __launch_bounds__(kThreads, 3) digit_pass_kernel(
         const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint64_t* __restrict__ keys_out,
         uint32_t* __restrict__ vals_out, const int n, const int shift, const int pass,
@@ -176,170 +179,179 @@ namespace nbg
         __shared__ int tile_s;
 
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        if (threadIdx.x == 0)
-            tile_s = static_cast<int>(atomicAdd(ticket, 1u));
-        for (int d = threadIdx.x; d < kWarps * kDigits / 2; d += kThreads)
-            warp_cnt2[d] = 0;
-        __syncthreads();
-        const int tile = tile_s;
-        const int tile_base = tile * kTile;
-        const int tile_n = min(kTile, n - tile_base);
-        const int base = tile_base + warp * (kTile / kWarps);
-        const unsigned lt = (1u << lane) - 1u;
+        const int tiles = (n + kTile - 1) / kTile;
+        for (;;)
+        {
+            if (threadIdx.x == 0)
+                tile_s = static_cast<int>(atomicAdd(ticket, 1u));
+            for (int d = threadIdx.x; d < kWarps * kDigits / 2; d += kThreads)
+                warp_cnt2[d] = 0;
+            __syncthreads();
+            const int tile = tile_s;
+            if (tile >= tiles)
+                break;
+            const int tile_base = tile * kTile;
+            const int tile_n = min(kTile, n - tile_base);
+            const int base = tile_base + warp * (kTile / kWarps);
+            const unsigned lt = (1u << lane) - 1u;
 
-        // load and rank (out-of-range lanes take digit kDigits, which no key has: they are
-        // matched among themselves, counted nowhere and never written)
-        uint64_t key[kRounds];
-        uint32_t rank[kRounds];
+            // load and rank (out-of-range lanes take digit kDigits, which no key has: they are
+            // matched among themselves, counted nowhere and never written)
+            uint64_t key[kRounds];
+            uint32_t rank[kRounds];
 #pragma unroll
-        for (int r = 0; r < kRounds; ++r)
-        {
-            const int i = base + r * 32 + lane;
-            key[r] = i < n ? keys[i] : 0ull;
-        }
-#pragma unroll
-        for (int r = 0; r < kRounds; ++r)
-        {
-            const bool ok = base + r * 32 + lane < n;
-            const unsigned d = ok ? static_cast<unsigned>((key[r] >> shift) & kMask) : static_cast<unsigned>(kDigits);
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
-            const int leader = __ffs(peers) - 1;
-            uint32_t before = 0;
-            if (lane == leader && ok)
+            for (int r = 0; r < kRounds; ++r)
             {
-                // counter warp * kDigits + d is the (d & 1) half of word (warp * kDigits + d) / 2
-                const unsigned half = (d & 1u) * 16u;
-                const uint32_t old = atomicAdd(&warp_cnt2[(warp * kDigits + static_cast<int>(d)) >> 1],
-                                               static_cast<uint32_t>(__popc(peers)) << half);
-                before = (old >> half) & 0xffffu;
+                const int i = base + r * 32 + lane;
+                key[r] = i < n ? keys[i] : 0ull;
             }
-            rank[r] = __shfl_sync(0xffffffffu, before, leader) + __popc(peers & lt);
-        }
-        __syncthreads();
+#pragma unroll
+            for (int r = 0; r < kRounds; ++r)
+            {
+                const bool ok = base + r * 32 + lane < n;
+                const unsigned d = ok ? static_cast<unsigned>((key[r] >> shift) & kMask) : static_cast<unsigned>(kDigits);
+                const unsigned peers = __match_any_sync(0xffffffffu, d);
+                const int leader = __ffs(peers) - 1;
+                uint32_t before = 0;
+                if (lane == leader && ok)
+                {
+                    // counter warp * kDigits + d is the (d & 1) half of word (warp * kDigits + d) / 2
+                    const unsigned half = (d & 1u) * 16u;
+                    const uint32_t old = atomicAdd(&warp_cnt2[(warp * kDigits + static_cast<int>(d)) >> 1],
+                                                   static_cast<uint32_t>(__popc(peers)) << half);
+                    before = (old >> half) & 0xffffu;
+                }
+                rank[r] = __shfl_sync(0xffffffffu, before, leader) + __popc(peers & lt);
+            }
+            __syncthreads();
 
-        // per digit: the count in earlier warps (warp_cnt becomes exclusive over warps) and
-        // the tile's total
-        uint32_t total[kPer];
-#pragma unroll
-        for (int q = 0; q < kPer; ++q)
-        {
-            const int d = threadIdx.x * kPer + q;
-            uint32_t run = 0;
-#pragma unroll
-            for (int w = 0; w < kWarps; ++w)
-            {
-                const uint32_t c = warp_cnt[w * kDigits + d];
-                warp_cnt[w * kDigits + d] = static_cast<uint16_t>(run);    // < kTile
-                run += c;
-            }
-            total[q] = run;
-        }
-        // publish this tile's counts at once: later tiles may already be waiting for them
-        const uint64_t epoch = static_cast<uint64_t>(pass + 1) << 32;
-#pragma unroll
-        for (int q = 0; q < kPer; ++q)
-        {
-            const int d = threadIdx.x * kPer + q;
-            store_relaxed(&status[static_cast<size_t>(tile) * kDigits + d],
-                          (tile == 0 ? kFlagInclusive : kFlagAggregate) | epoch | total[q]);
-        }
-        // where each digit starts within the tile, and where it starts in the output
-        {
-            uint32_t start[kPer], gcount[kPer], gstart[kPer];
-            block_exclusive(total, start, warp_sum[0]);
-#pragma unroll
-            for (int q = 0; q < kPer; ++q)
-                gcount[q] = ghist[threadIdx.x * kPer + q];
-            block_exclusive(gcount, gstart, warp_sum[1]);
-#pragma unroll
-            for (int q = 0; q < kPer; ++q)
-            {
-                digit_start[threadIdx.x * kPer + q] = start[q];
-                gbase[threadIdx.x * kPer + q] = gstart[q];
-            }
-        }
-        // decoupled look-back: sum the earlier tiles' counts of each digit, four tiles per
-        // step, back to the nearest tile that has published an inclusive count
-        if (tile > 0)
-        {
+            // per digit: the count in earlier warps (warp_cnt becomes exclusive over warps) and
+            // the tile's total
+            uint32_t total[kPer];
 #pragma unroll
             for (int q = 0; q < kPer; ++q)
             {
                 const int d = threadIdx.x * kPer + q;
-                uint32_t before = 0;
-                int j = tile - 1;
-                uint64_t t0 = 0;
-                while (j >= 0)
+                uint32_t run = 0;
+#pragma unroll
+                for (int w = 0; w < kWarps; ++w)
                 {
-                    uint64_t w[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-                        w[u] = j - u >= 0 ? load_relaxed(&status[static_cast<size_t>(j - u) * kDigits + d]) : 0ull;
-                    // take the words in order while they are published aggregates; stop at
-                    // an inclusive one, or wait where one is not published yet
-                    int u = 0;
-                    bool done = false;
-                    for (; u < 4 && j - u >= 0; ++u)
-                    {
-                        if ((w[u] & ~(3ull << 62)) >> 32 != static_cast<uint64_t>(pass + 1) || !(w[u] >> 62))
-                            break;
-                        before += static_cast<uint32_t>(w[u]);
-                        if ((w[u] >> 62) == 2)
-                        {
-                            done = true;
-                            break;
-                        }
-                    }
-                    if (done)
-                        break;
-                    j -= u;
-                    if (j >= 0 && u == 0)
-                    {
-                        // tile j has not published yet: it is running and will
-                        if (!t0)
-                            t0 = globaltimer();
-                        else if (globaltimer() - t0 > kWaitLimitNs)
-                        {
-                            atomicOr(err, DEV_ERR_TIMEOUT);
-                            break;
-                        }
-                        __nanosleep(100);
-                    }
+                    const uint32_t c = warp_cnt[w * kDigits + d];
+                    warp_cnt[w * kDigits + d] = static_cast<uint16_t>(run);    // < kTile
+                    run += c;
                 }
-                store_relaxed(&status[static_cast<size_t>(tile) * kDigits + d],
-                              kFlagInclusive | epoch | (before + total[q]));
-                gbase[d] += before;
+                total[q] = run;
             }
-        }
-        __syncthreads();
-
-        // stage the tile in digit order
+            // publish this tile's counts at once: later tiles may already be waiting for them
+            const uint64_t epoch = static_cast<uint64_t>(pass + 1) << 32;
 #pragma unroll
-        for (int r = 0; r < kRounds; ++r)
-        {
-            const int i = base + r * 32 + lane;
-            if (i >= n)
-                continue;
-            const unsigned d = static_cast<unsigned>((key[r] >> shift) & kMask);
-            const uint32_t pos = digit_start[d] + warp_cnt[warp * kDigits + d] + rank[r];
-            stage_k[pos] = key[r];
-            stage_v[pos] = vals[i];
-        }
-        __syncthreads();
-        // write out in staged order: consecutive threads take consecutive staged keys, which
-        // within a digit go to consecutive output positions
-        for (int s = threadIdx.x; s < tile_n; s += kThreads)
-        {
-            const uint64_t k = stage_k[s];
-            const unsigned d = static_cast<unsigned>((k >> shift) & kMask);
-            const uint32_t pos = gbase[d] + (static_cast<uint32_t>(s) - digit_start[d]);
-            if (pos < static_cast<uint32_t>(n))     // always, unless a look-back wait gave up
+            for (int q = 0; q < kPer; ++q)
             {
-                keys_out[pos] = k;
-                vals_out[pos] = stage_v[s];
+                const int d = threadIdx.x * kPer + q;
+                store_relaxed(&status[static_cast<size_t>(tile) * kDigits + d],
+                              (tile == 0 ? kFlagInclusive : kFlagAggregate) | epoch | total[q]);
             }
-            else
-                atomicOr(err, DEV_ERR_BOUNDS);
+            // where each digit starts within the tile, and where it starts in the output
+            {
+                uint32_t start[kPer], gcount[kPer], gstart[kPer];
+                block_exclusive(total, start, warp_sum[0]);
+#pragma unroll
+                for (int q = 0; q < kPer; ++q)
+                    gcount[q] = ghist[threadIdx.x * kPer + q];
+                block_exclusive(gcount, gstart, warp_sum[1]);
+#pragma unroll
+                for (int q = 0; q < kPer; ++q)
+                {
+                    digit_start[threadIdx.x * kPer + q] = start[q];
+                    gbase[threadIdx.x * kPer + q] = gstart[q];
+                }
+            }
+            // decoupled look-back: sum the earlier tiles' counts of each digit, four tiles per
+            // step, back to the nearest tile that has published an inclusive count
+            if (tile > 0)
+            {
+#pragma unroll
+                for (int q = 0; q < kPer; ++q)
+                {
+                    const int d = threadIdx.x * kPer + q;
+                    uint32_t before = 0;
+                    int j = tile - 1;
+                    uint64_t t0 = 0;
+                    while (j >= 0)
+                    {
+                        uint64_t w[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            w[u] = j - u >= 0 ? load_relaxed(&status[static_cast<size_t>(j - u) * kDigits + d]) : 0ull;
+                        // take the words in order while they are published aggregates; stop at
+                        // an inclusive one, or wait where one is not published yet
+                        int u = 0;
+                        bool done = false;
+                        for (; u < 4 && j - u >= 0; ++u)
+                        {
+                            if ((w[u] & ~(3ull << 62)) >> 32 != static_cast<uint64_t>(pass + 1) || !(w[u] >> 62))
+                                break;
+                            before += static_cast<uint32_t>(w[u]);
+                            if ((w[u] >> 62) == 2)
+                            {
+                                done = true;
+                                break;
+                            }
+                        }
+                        if (done)
+                            break;
+                        j -= u;
+                        if (j >= 0 && u == 0)
+                        {
+                            // tile j has not published yet: it is running and will
+                            if (!t0)
+                                t0 = globaltimer();
+                            else if (globaltimer() - t0 > kWaitLimitNs)
+                            {
+                                atomicOr(err, DEV_ERR_TIMEOUT);
+                                break;
+                            }
+                            __nanosleep(100);
+                        }
+                    }
+                    store_relaxed(&status[static_cast<size_t>(tile) * kDigits + d],
+                                  kFlagInclusive | epoch | (before + total[q]));
+                    gbase[d] += before;
+                }
+            }
+            __syncthreads();
+
+            // stage the tile in digit order
+#pragma unroll
+            for (int r = 0; r < kRounds; ++r)
+            {
+                const int i = base + r * 32 + lane;
+                if (i >= n)
+                    continue;
+                const unsigned d = static_cast<unsigned>((key[r] >> shift) & kMask);
+                const uint32_t pos = digit_start[d] + warp_cnt[warp * kDigits + d] + rank[r];
+                stage_k[pos] = key[r];
+                stage_v[pos] = vals[i];
+            }
+            __syncthreads();
+            // write out in staged order: consecutive threads take consecutive staged keys, which
+            // within a digit go to consecutive output positions
+            for (int s = threadIdx.x; s < tile_n; s += kThreads)
+            {
+                const uint64_t k = stage_k[s];
+                const unsigned d = static_cast<unsigned>((k >> shift) & kMask);
+                const uint32_t pos = gbase[d] + (static_cast<uint32_t>(s) - digit_start[d]);
+                if (pos < static_cast<uint32_t>(n))     // always, unless a look-back wait gave up
+                {
+                    keys_out[pos] = k;
+                    vals_out[pos] = stage_v[s];
+                }
+                else
+                    atomicOr(err, DEV_ERR_BOUNDS);
+            }
+            if (!PERSIST)
+                break;
+            __syncthreads();        // shared memory is the next tile's
         }
     }
 
@@ -362,12 +374,27 @@ namespace nbg
         const int passes = (end_bit - begin_bit + kBits - 1) / kBits;
         if (passes < 1 || pass_base < 0 || pass_base + passes > kMaxPasses)
             return cudaErrorInvalidValue;
-        static const cudaError_t attr = cudaFuncSetAttribute(
-            digit_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kPassSmem));
+        static const cudaError_t attr = [] {
+            const cudaError_t a = cudaFuncSetAttribute(digit_pass_kernel<false>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       static_cast<int>(kPassSmem));
+            return a != cudaSuccess ? a
+                                    : cudaFuncSetAttribute(digit_pass_kernel<true>,
+                                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                           static_cast<int>(kPassSmem));
+        }();
         if (attr != cudaSuccess)
             return attr;
         const int tiles = static_cast<int>((n + kTile - 1) / kTile);
         const TempLayout t = layout(temp, static_cast<size_t>(tiles));
+        // a call that may do nothing (run_if) launches persistent passes, one CTA per
+        // resident slot, so that a pass with nothing to do costs few CTAs; otherwise one CTA
+        // per tile
+        static const int per_sm = [] {
+            int b = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, digit_pass_kernel<true>, kThreads, kPassSmem);
+            return std::max(1, b);
+        }();
         // the first call zeroes the tickets, histograms and published counts of every pass;
         // a later call's passes have their own tickets and histograms, and their counts carry
         // other epochs
@@ -378,6 +405,7 @@ namespace nbg
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int hist_grid = std::max(1, std::min((static_cast<int>(n) + kHistThreads - 1) / kHistThreads, 2 * sms));
+        const int pass_grid = std::min(tiles, per_sm * sms);
         digit_hist_kernel<<<hist_grid, kHistThreads, 0, stream>>>(keys, static_cast<int>(n), begin_bit, passes,
                                                                   t.ghist + pass_base * kDigits, run_if);
         ++*launches;
@@ -391,9 +419,14 @@ namespace nbg
         for (int p = 0; p < passes; ++p)
         {
             const int q = pass_base + p;
-            digit_pass_kernel<<<tiles, kThreads, kPassSmem, stream>>>(kin, vin, kout, vout, static_cast<int>(n),
-                                                                       begin_bit + p * kBits, q, t.ghist + q * kDigits,
-                                                                       t.status, t.tickets + q, err, run_if);
+            if (run_if)
+                digit_pass_kernel<true><<<pass_grid, kThreads, kPassSmem, stream>>>(
+                    kin, vin, kout, vout, static_cast<int>(n), begin_bit + p * kBits, q, t.ghist + q * kDigits,
+                    t.status, t.tickets + q, err, run_if);
+            else
+                digit_pass_kernel<false><<<tiles, kThreads, kPassSmem, stream>>>(
+                    kin, vin, kout, vout, static_cast<int>(n), begin_bit + p * kBits, q, t.ghist + q * kDigits,
+                    t.status, t.tickets + q, err, run_if);
             ++*launches;
             e = cudaGetLastError();
             if (e != cudaSuccess)
