@@ -5,10 +5,11 @@
 //   0. digit_hist: one read of the keys histograms the digits of every pass at once (a
 //      key's digits do not depend on the order of the keys), into ghist[pass][digit].
 //   1. digit_pass (once per pass): a CTA takes the next 4096-key tile in launch order (an
-//      atomic ticket), ranks its keys stably, publishes its per-digit counts, and finds
-//      how many keys of each digit the earlier tiles hold by decoupled look-back over
-//      their published counts. The tile is staged in shared memory in digit order and
-//      written out so that each digit's run lands contiguously (coalesced stores).
+//      atomic ticket), ranks its keys stably, publishes its per-digit counts, stages the
+//      tile in shared memory in digit order, and then finds how many keys of each digit
+//      the earlier tiles hold by decoupled look-back over their published counts (staging
+//      first gives those tiles time to publish). The tile is written out so that each
+//      digit's run lands contiguously (coalesced stores).
 // The look-back only waits on tiles whose tickets were taken earlier, by CTAs that are
 // already running and that publish their counts before they wait themselves, so the wait
 // always ends; it is still bounded in time, and a wait that gives up records
@@ -266,6 +267,20 @@ namespace nbg
                     gbase[threadIdx.x * kPer + q] = gstart[q];
                 }
             }
+            // stage the tile in digit order: it needs only the tile's own counts, and done
+            // before the look-back it gives the earlier tiles time to publish theirs
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < kRounds; ++r)
+            {
+                const int i = base + r * 32 + lane;
+                if (i >= n)
+                    continue;
+                const unsigned d = static_cast<unsigned>((key[r] >> shift) & kMask);
+                const uint32_t pos = digit_start[d] + warp_cnt[warp * kDigits + d] + rank[r];
+                stage_k[pos] = key[r];
+                stage_v[pos] = vals[i];
+            }
             // decoupled look-back: sum the earlier tiles' counts of each digit, four tiles per
             // step, back to the nearest tile that has published an inclusive count
             if (tile > 0)
@@ -321,19 +336,6 @@ namespace nbg
             }
             __syncthreads();
 
-            // stage the tile in digit order
-#pragma unroll
-            for (int r = 0; r < kRounds; ++r)
-            {
-                const int i = base + r * 32 + lane;
-                if (i >= n)
-                    continue;
-                const unsigned d = static_cast<unsigned>((key[r] >> shift) & kMask);
-                const uint32_t pos = digit_start[d] + warp_cnt[warp * kDigits + d] + rank[r];
-                stage_k[pos] = key[r];
-                stage_v[pos] = vals[i];
-            }
-            __syncthreads();
             // write out in staged order: consecutive threads take consecutive staged keys, which
             // within a digit go to consecutive output positions
             for (int s = threadIdx.x; s < tile_n; s += kThreads)
