@@ -14,7 +14,8 @@
 //      coordinate is below the centre: reference octant = digit ^ 7;
 //   3. radix_sort_pairs over (code, index): stable, so ties keep index order;
 //   4. gather_sum_kernel: bodies into Morton order, and exact fixed-point (int64) prefix
-//      sums of m and m*x, whose differences give each cell's mass and COM, in one pass;
+//      sums of m and m*x within tiles of sorted bodies, plus a scan of the tile totals:
+//      differences of their sums give each cell's mass and COM;
 //   5. karras_kernel: binary radix tree over the sorted codes (Karras 2012), duplicates
 //      separated by index; each internal node's common-prefix length fixes its octree
 //      level floor(prefix / 3) (capped at 21, the last Morton level), and the node is
@@ -89,7 +90,8 @@ namespace nbg
         int* prefix = nullptr;          // common-prefix bits of each internal node
         uint32_t* octflag = nullptr;
         uint32_t* octidx = nullptr;
-        Int64x4* psum = nullptr;        // N + 1 fixed-point prefix sums of {m x, m y, m z, m}
+        Int64x4* psum = nullptr;        // N + 1 fixed-point sums of {m x, m y, m z, m} over the
+                                        // sorted bodies before x within x's cell-sum tile
         OctNode* nodes = nullptr;
         void* temp = nullptr;           // sort and scan temporaries
         size_t temp_bytes = 0;
@@ -506,68 +508,30 @@ namespace nbg
         return Int64x4{ a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w };
     }
 
-    __device__ __forceinline__ unsigned load_acquire(const unsigned* p)
-    {
-        unsigned v;
-        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-        return v;
-    }
-
-    __device__ __forceinline__ void store_release(unsigned* p, const unsigned v)
-    {
-        asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
-    }
-
-    __device__ __forceinline__ Int64x4 load_cg(const Int64x4* p)
-    {
-        const longlong2* q = reinterpret_cast<const longlong2*>(p);
-        const longlong2 a = __ldcg(q), b = __ldcg(q + 1);
-        return Int64x4{ a.x, a.y, b.x, b.y };
-    }
-
-    __device__ __forceinline__ Int64x4 shfl_idx4(const Int64x4 v, const int src)
-    {
-        return Int64x4{ __shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
-                        __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src) };
-    }
-
-    // Tile states of the single-pass scan: a tile's total published, or the total of it and
-    // every earlier tile.
-    constexpr unsigned kTileAggregate = 1u, kTileInclusive = 2u;
-
     // Bodies into Morton order (pos_mass, and the radius when srad is given: only the cutoff
-    // law reads it) and psum[k] = the sum of the terms of sorted bodies 0 .. k-1, k = 0 .. n,
-    // in one pass. A CTA takes the next 4096-body tile in launch order (a ticket), gathers it
-    // (four consecutive bodies per thread), scans its terms, publishes its total, and finds
-    // the total of the earlier tiles by decoupled look-back (Merrill & Garland 2016): warp 0
-    // reads 32 earlier tiles' states at a time and sums back to the nearest tile whose
-    // running total is published. Tiles wait only on tiles with earlier tickets, which are
-    // already running, so the wait ends; it is bounded all the same, and a wait that gives
-    // up records DEV_ERR_TIMEOUT. The sums are integers, so the result does not depend on
-    // which tiles published what when.
+    // law reads it), and the fixed-point prefix sums within each tile of kMomTile sorted
+    // bodies: part[x] = the sum of the terms of the bodies of x's tile before x, for
+    // x = 0 .. n (x = n belongs to tile n / kMomTile, which is past the last tile, and has
+    // sum 0, when n is a multiple of the tile). Each tile's total goes to tile_sum; the sum
+    // of all bodies before x is then tile_prefix[x / kMomTile] + part[x], with tile_prefix
+    // the exclusive scan of the totals (a tile past the last has total 0). Tiles need not
+    // wait for one another. Four consecutive bodies per thread; every random read is issued
+    // before any is used (indices past the end read the last body and are not stored).
     __global__ void __launch_bounds__(kMomThreads) gather_sum_kernel(
         const float4* __restrict__ src, const int stride, const float4* __restrict__ vel_radius,
         const uint32_t* __restrict__ order, const int n, const BoxParams* __restrict__ box,
-        float4* __restrict__ spm, float* __restrict__ srad, Int64x4* __restrict__ psum,
-        Int64x4* __restrict__ tile_agg, Int64x4* __restrict__ tile_incl, unsigned* __restrict__ tile_state,
-        unsigned* __restrict__ ticket, unsigned* __restrict__ err)
+        float4* __restrict__ spm, float* __restrict__ srad, Int64x4* __restrict__ part,
+        Int64x4* __restrict__ tile_sum)
     {
         using Op = ScanOps<Int64x4>;
         if (n <= 0)
             return;
         __shared__ Int64x4 warp_tot[kMomThreads / 32];
-        __shared__ Int64x4 tile_prefix;
-        __shared__ int tile_s;
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        if (threadIdx.x == 0)
-            tile_s = static_cast<int>(atomicAdd(ticket, 1u));
-        __syncthreads();
-        const int tile = tile_s;
+        const int tile = blockIdx.x;
         const int mass_shift = box->mass_shift, mom_shift = box->mom_shift;
         const int base = tile * kMomTile + threadIdx.x * kMomItems;
 
-        // gather: every random read is issued before any is used (indices past the end read
-        // the last body and are not stored)
         uint32_t idx[kMomItems];
         if (base + kMomItems <= n)
         {
@@ -643,69 +607,13 @@ namespace nbg
             }
             if (lane < kWarpsPerTile)
                 warp_tot[lane] = wi;    // inclusive over warps
-            const Int64x4 agg = shfl_idx4(wi, 31);      // the tile's total
-            // publish the tile's own total at once: later tiles may be waiting for it
-            if (lane == 0)
-            {
-                if (tile == 0)
-                    tile_incl[0] = agg;
-                else
-                    tile_agg[tile] = agg;
-                __threadfence();
-                store_release(&tile_state[tile], tile == 0 ? kTileInclusive : kTileAggregate);
-            }
-            Int64x4 before{ 0, 0, 0, 0 };
-            int j = tile - 1;           // the latest tile not yet summed
-            uint64_t t0 = 0;
-            while (j >= 0)
-            {
-                const int jj = j - lane;
-                const unsigned st = jj >= 0 ? load_acquire(&tile_state[jj]) : kTileInclusive;
-                const unsigned incl_mask = __ballot_sync(0xffffffffu, st == kTileInclusive);
-                const unsigned none_mask = __ballot_sync(0xffffffffu, st == 0u);
-                // lanes up to and including the first inclusive one are the ones summed
-                const int first = incl_mask ? __ffs(incl_mask) - 1 : 31;
-                const unsigned need = first == 31 ? 0xffffffffu : (2u << first) - 1u;
-                if (none_mask & need)
-                {
-                    if (!t0)
-                        t0 = globaltimer();
-                    else if (globaltimer() - t0 > kWaitLimitNs)
-                    {
-                        if (lane == 0)
-                            atomicOr(err, DEV_ERR_TIMEOUT);
-                        break;
-                    }
-                    __nanosleep(64);
-                    continue;
-                }
-                Int64x4 val{ 0, 0, 0, 0 };
-                if (lane <= first && jj >= 0)
-                    val = load_cg(st == kTileInclusive ? &tile_incl[jj] : &tile_agg[jj]);
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1)
-                    val = add4(val, Op::shfl_down(val, d));
-                before = add4(before, shfl_idx4(val, 0));     // lane 0 holds the sum
-                if (incl_mask)
-                    break;
-                j -= 32;
-            }
-            if (lane == 0)
-            {
-                if (tile > 0)
-                {
-                    tile_incl[tile] = add4(before, agg);
-                    __threadfence();
-                    store_release(&tile_state[tile], kTileInclusive);
-                }
-                tile_prefix = before;
-            }
+            if (lane == 31)
+                tile_sum[tile] = wi;    // the tile's total
         }
         __syncthreads();
-        Int64x4 excl = Op::shfl_up(incl, 1);
+        Int64x4 off = Op::shfl_up(incl, 1);
         if (lane == 0)
-            excl = Int64x4{ 0, 0, 0, 0 };
-        Int64x4 off = add4(tile_prefix, excl);
+            off = Int64x4{ 0, 0, 0, 0 };
         if (warp > 0)
             off = add4(off, warp_tot[warp - 1]);
 #pragma unroll
@@ -714,12 +622,16 @@ namespace nbg
             const int i = base + k;
             if (i < n)
             {
-                psum[i] = off;
+                part[i] = off;
                 off = add4(off, body_terms(p[k], mass_shift, mom_shift));
             }
         }
         if (base <= n - 1 && n - 1 < base + kMomItems)
-            psum[n] = off;
+        {
+            const int past = (n % kMomTile) == 0 ? 1 : 0;    // x = n opens the tile past the last
+            part[n] = past ? Int64x4{ 0, 0, 0, 0 } : off;
+            tile_sum[tile + 1] = Int64x4{ 0, 0, 0, 0 };      // past the last tile: total 0
+        }
     }
 
     // ------------------------------------------------------------------------------------
@@ -892,8 +804,9 @@ namespace nbg
     // idling on unflagged ones.
     __global__ void __launch_bounds__(256) octnode_kernel(const int2* __restrict__ child, const int2* __restrict__ range,
                                    const int* __restrict__ prefix, const uint32_t* __restrict__ flag,
-                                   const uint32_t* __restrict__ octidx, const Int64x4* __restrict__ psum,
-                                   const int m, const BoxParams* __restrict__ box, const float theta,
+                                   const uint32_t* __restrict__ octidx, const Int64x4* __restrict__ part,
+                                   const Int64x4* __restrict__ tile_prefix, const int m,
+                                   const BoxParams* __restrict__ box, const float theta,
                                    OctNode* __restrict__ nodes, unsigned* __restrict__ err,
                                    unsigned long long* __restrict__ stats)
     {
@@ -932,7 +845,9 @@ namespace nbg
             const int2 rg = range[i];
             const int pre = prefix[i];
             const int lvl = level_of(pre);
-            const Int64x4 hi = psum[rg.y + 1], lo = psum[rg.x];
+            // the sums before the cell's first body and after its last: exact integers
+            const Int64x4 hi = add4(tile_prefix[(rg.y + 1) / kMomTile], part[rg.y + 1]);
+            const Int64x4 lo = add4(tile_prefix[rg.x / kMomTile], part[rg.x]);
             const long long ms = hi.w - lo.w;   // exact: the cell's own terms
             OctNode* out = nodes + octidx[i];
             float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1789,11 +1704,12 @@ namespace nbg
                 return st;
             const size_t cap = std::max(n, b.cap + b.cap / 2);
             const size_t tiles = (cap + kMomTile - 1) / kMomTile;
-            // the sort's temporaries; the cell sums' tile totals, running totals, states and
-            // ticket; the octree compaction's scan
+            // the sort's temporaries; later the cell sums' tile totals and tile prefixes, and
+            // after them the scans' temporaries (the tile totals' and the octree compaction's)
             const size_t tb = std::max(sort_temp_bytes(cap),
-                                       std::max(2 * tiles * sizeof(Int64x4) + (tiles + 1) * sizeof(unsigned),
-                                                scan_temp_elems(cap) * sizeof(uint32_t)));
+                                       2 * (tiles + 1) * sizeof(Int64x4)
+                                           + std::max(scan_temp_elems(tiles + 1) * sizeof(Int64x4),
+                                                      scan_temp_elems(cap) * sizeof(uint32_t)));
             cudaError_t e = cudaSuccess;
             cudaStream_t s = ctx->stream;
             for (int k = 0; k < 2 && e == cudaSuccess; ++k)
@@ -1894,19 +1810,20 @@ namespace nbg
         b.order = order;
         b.codes = keys;
         const unsigned tiles = std::max(1u, ceil_div(n, kMomTile));
-        Int64x4* tile_agg = static_cast<Int64x4*>(b.temp);
-        Int64x4* tile_incl = tile_agg + tiles;
-        unsigned* tile_state = reinterpret_cast<unsigned*>(tile_incl + tiles);      // + the ticket
-        e = cudaMemsetAsync(tile_state, 0, (tiles + 1) * sizeof(unsigned), s);
-        if (e != cudaSuccess)
-            return ctx_cuda_fail(ctx, e, "cell sums");
+        // temporaries: tile totals and their exclusive scan (tiles + 1 each: the entry past
+        // the last tile gives the sum of all bodies), then the scans' own
+        Int64x4* tile_sum = static_cast<Int64x4*>(b.temp);
+        Int64x4* tile_prefix = tile_sum + tiles + 1;
+        void* scan_temp = tile_prefix + tiles + 1;
         const bool radius = p->law == NBODY_LAW_CUTOFF;
         gather_sum_kernel<<<tiles, kMomThreads, 0, s>>>(src, stride,
                                                         radius && ctx->layout != NBODY_LAYOUT_AOS ? ctx->vr : nullptr,
                                                         order, ni, b.box, b.spm, radius ? b.srad : nullptr, b.psum,
-                                                        tile_agg, tile_incl, tile_state, tile_state + tiles,
-                                                        ctx->dev_error);
+                                                        tile_sum);
         ++L;
+        e = exclusive_scan<Int64x4>(tile_sum, tile_prefix, tiles + 1, static_cast<Int64x4*>(scan_temp), s, &L);
+        if (e != cudaSuccess)
+            return ctx_cuda_fail(ctx, e, "cell sums");
         if (n < 2)
         {
             b.built = true;
@@ -1918,11 +1835,12 @@ namespace nbg
         karras_kernel<<<ceil_div(m, kKarrasThreads), kKarrasThreads, 0, s>>>(keys, ni, b.child, b.range, b.prefix,
                                                                             b.octflag);
         ++L;
-        e = exclusive_scan<uint32_t>(b.octflag, b.octidx, m, static_cast<uint32_t*>(b.temp), s, &L);
+        e = exclusive_scan<uint32_t>(b.octflag, b.octidx, m, static_cast<uint32_t*>(scan_temp), s, &L);
         if (e != cudaSuccess)
             return ctx_cuda_fail(ctx, e, "octree compaction");
-        octnode_kernel<<<ceil_div(m, 256 * kOctSpan), 256, 0, s>>>(b.child, b.range, b.prefix, b.octflag, b.octidx, b.psum, m, b.box,
-                                                         p->theta, b.nodes, ctx->dev_error, b.stats);
+        octnode_kernel<<<ceil_div(m, 256 * kOctSpan), 256, 0, s>>>(b.child, b.range, b.prefix, b.octflag, b.octidx,
+                                                                    b.psum, tile_prefix, m, b.box, p->theta, b.nodes,
+                                                                    ctx->dev_error, b.stats);
         ++L;
         e = cudaGetLastError();
         if (e != cudaSuccess)
