@@ -73,7 +73,7 @@ namespace nbg
         // bodies, whose longest is 10) instead makes the build finish with a full sort.
         constexpr int kRunShift = 18;
         constexpr int kMaxRun = 32;
-        constexpr int kMomThreads = 1024;
+        constexpr int kMomThreads = 512;
         constexpr int kMomItems = 4;
         constexpr int kMomTile = kMomThreads * kMomItems;   // bodies per cell-sum tile
     }
@@ -801,8 +801,8 @@ namespace nbg
     // One octree record per flagged binary node. Latency bound (chains of dependent loads),
     // so a warp first gathers the flagged nodes among 32 * kOctSpan consecutive binary nodes
     // (ballots; about 40 % are flagged) and its lanes then take them in turn, instead of
-    // idling on unflagged ones.
-    __global__ void __launch_bounds__(256) octnode_kernel(const int2* __restrict__ child, const int2* __restrict__ range,
+    // idling on unflagged ones; and full occupancy (32 registers) beats fewer spills.
+    __global__ void __launch_bounds__(256, 8) octnode_kernel(const int2* __restrict__ child, const int2* __restrict__ range,
                                    const int* __restrict__ prefix, const uint32_t* __restrict__ flag,
                                    const uint32_t* __restrict__ octidx, const Int64x4* __restrict__ part,
                                    const Int64x4* __restrict__ tile_prefix, const int m,
