@@ -417,9 +417,12 @@ def bench_compensated(torch, stream, flush, native, bodies, args, fp32_value, fp
 # |com - x| > size * theta, bhtree.cpp:117-125): conventional theta = 1 / reference theta.
 BH_THETAS = (("theta_0.5", 0.5), ("theta_0.75", 0.75), ("theta_conventional_0.5", 2.0),
              ("theta_conventional_0.75", 4.0 / 3.0))
-# compulsory HBM bytes per body of the build (byte model): bbox 16, Morton 16 + 8,
-# sort 7 passes x 24, permute 32, tree ~56 per internal node, COM ~48 per node
-BUILD_BYTES_PER_BODY = 16 + 24 + 7 * 24 + 32 + 56 + 48
+# compulsory HBM bytes per body of the build (byte model): bounding box 16; Morton codes 16
+# read + 12 written; sort: histogram 8, five 9-bit passes x 24, run ordering 12; gather and
+# cell sums: order 4 + body 16 + sorted body 16 + prefix 32; radix tree: keys 8 + records 24;
+# octree numbering 8; octree records ~70 (0.45 cells per body, each 64 B written and 84 B of
+# ranges, prefixes and sums read, and the flags)
+BUILD_BYTES_PER_BODY = 16 + 28 + (8 + 5 * 24 + 12) + (4 + 16 + 16 + 32) + (8 + 24) + 8 + 70
 
 
 def bh_run(torch, stream, flush, native, ctx, bodies, p, steps, warmup, a64, tg, fp32_peak, hbm):
