@@ -16,10 +16,10 @@
 //   4. gather_sum_kernel: bodies into Morton order, and exact fixed-point (int64) prefix
 //      sums of m and m*x within tiles of sorted bodies, plus a scan of the tile totals:
 //      differences of their sums give each cell's mass and COM;
-//   5. karras_kernel: binary radix tree over the sorted codes (Karras 2012), duplicates
-//      separated by index; each internal node's common-prefix length fixes its octree
-//      level floor(prefix / 3) (capped at 21, the last Morton level), and the node is
-//      flagged as an octree node here;
+//   5. adjacent_prefix_kernel, radix_near_kernel, radix_far_kernel: binary radix tree over
+//      the sorted codes (Karras 2012), duplicates separated by index; each internal node's
+//      common-prefix length fixes its octree level floor(prefix / 3) (capped at 21, the
+//      last Morton level), and the node is flagged as an octree node here;
 //   6. octree nodes = binary nodes whose level exceeds their parent's (plus the root).
 //      A reference cell whose bodies all sit in one octant (a chain of single-child
 //      cells) has the same centre of mass and mass at every level of the chain, and the
@@ -637,96 +637,251 @@ namespace nbg
     // ------------------------------------------------------------------------------------
     // 5. binary radix tree (Karras 2012)
     // ------------------------------------------------------------------------------------
-    constexpr int kKarrasThreads = 256;
-    constexpr int kKarrasHalo = 256;        // keys staged on either side of a block's nodes
-    constexpr int kKarrasWin = kKarrasThreads + 2 * kKarrasHalo;
-
-    // The sorted keys around one block's nodes, staged in shared memory: the searches of most
-    // nodes stay within kKarrasHalo keys of the node, and read there instead of through the
-    // cache hierarchy; a probe outside the window reads global memory.
-    struct KeyWindow
+    // common-prefix length of sorted keys i and j (0 <= i < n), duplicates separated by
+    // index (64 + the index bits they share); -1 for j outside [0, n)
+    __device__ __forceinline__ int delta(const uint64_t* __restrict__ keys, const int n, const int i, const int j)
     {
-        const uint64_t* __restrict__ keys;
-        const uint64_t* win;
-        int w0;         // key index of win[0]
-        int n;
-
-        __device__ __forceinline__ uint64_t at(const int k) const
-        {
-            const unsigned t = static_cast<unsigned>(k - w0);
-            return t < static_cast<unsigned>(kKarrasWin) ? win[t] : keys[k];
-        }
-
-        // common-prefix length of keys i and j (0 <= i < n), duplicates separated by index;
-        // -1 for j outside [0, n)
-        __device__ __forceinline__ int delta(const uint64_t a, const int i, const int j) const
-        {
-            if (j < 0 || j >= n)
-                return -1;
-            const uint64_t b = at(j);
-            if (a != b)
-                return __clzll(static_cast<long long>(a ^ b));
-            return 64 + __clz(static_cast<int>(static_cast<unsigned>(i) ^ static_cast<unsigned>(j)));
-        }
-    };
+        if (j < 0 || j >= n)
+            return -1;
+        const uint64_t a = keys[i], b = keys[j];
+        if (a != b)
+            return __clzll(static_cast<long long>(a ^ b));
+        return 64 + __clz(static_cast<int>(static_cast<unsigned>(i) ^ static_cast<unsigned>(j)));
+    }
 
     __device__ __forceinline__ int level_of(const int prefix) { return min(kMaxLevel, prefix / 3); }
 
-    // Node i of the binary radix tree, and whether it is an octree node. A node's range
-    // [lo, hi] is bounded by two splits, delta(lo - 1, lo) and delta(hi, hi + 1), both below
-    // its own; its parent splits at the larger of the two (the smallest range that strictly
-    // contains [lo, hi] ends where the shared prefix first shortens), so the parent's
-    // prefix is known here without a parent array. A node is an octree node when its level
-    // exceeds its parent's, or it is the root.
-    __global__ void __launch_bounds__(kKarrasThreads) karras_kernel(
-        const uint64_t* __restrict__ keys, const int n, int2* __restrict__ child, int2* __restrict__ range,
-        int* __restrict__ prefix, uint32_t* __restrict__ flag)
+    // dl[k] = delta(k, k + 1) for k < n - 1: 1 .. 95, one byte. Four per thread. For sorted
+    // keys the common prefix of keys i < j is the least of dl[i .. j - 1].
+    __global__ void __launch_bounds__(256) adjacent_prefix_kernel(const uint64_t* __restrict__ keys, const int n,
+                                                                  uint8_t* __restrict__ dl)
     {
-        __shared__ uint64_t win[kKarrasWin];
-        const int w0 = static_cast<int>(blockIdx.x) * kKarrasThreads - kKarrasHalo;
-        for (int t = threadIdx.x; t < kKarrasWin; t += kKarrasThreads)
-        {
-            const int k = w0 + t;
-            if (k >= 0 && k < n)
-                win[t] = keys[k];
-        }
-        __syncthreads();
-        const KeyWindow kw{ keys, win, w0, n };
-        const int i = blockIdx.x * kKarrasThreads + threadIdx.x;
-        if (i >= n - 1)
+        const int k0 = (blockIdx.x * 256 + threadIdx.x) * 4;
+        if (k0 >= n - 1)
             return;
-        const uint64_t ki = win[i - w0];
-        const int d = (kw.delta(ki, i, i + 1) - kw.delta(ki, i, i - 1)) >= 0 ? 1 : -1;
-        const int dmin = kw.delta(ki, i, i - d);
-        int lmax = 2;
-        while (kw.delta(ki, i, i + lmax * d) > dmin)
-            lmax <<= 1;
-        int l = 0;
-        for (int t = lmax >> 1; t >= 1; t >>= 1)
-            if (kw.delta(ki, i, i + (l + t) * d) > dmin)
-                l += t;
-        const int j = i + l * d;
-        const int dnode = kw.delta(ki, i, j);
-        int s = 0;
-        for (int t = (l + 1) >> 1;; t = (t + 1) >> 1)
+        uint64_t a[5];
+#pragma unroll
+        for (int u = 0; u < 5; ++u)
+            a[u] = keys[min(k0 + u, n - 1)];
+        uint32_t packed = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
         {
-            if (kw.delta(ki, i, i + (s + t) * d) > dnode)
-                s += t;
-            if (t == 1)
-                break;
+            const int k = k0 + u;
+            const uint32_t v = a[u] != a[u + 1]
+                                   ? static_cast<uint32_t>(__clzll(static_cast<long long>(a[u] ^ a[u + 1])))
+                                   : 64u + static_cast<uint32_t>(__clz(k ^ (k + 1)));
+            packed |= (k < n - 1 ? v : 0u) << (8 * u);
         }
-        const int gamma = i + s * d + min(d, 0);
-        const int lo = min(i, j), hi = max(i, j);
-        const int left = (lo == gamma) ? ~gamma : gamma;
-        const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
-        child[i] = make_int2(left, right);
+        if (k0 + 4 <= n - 1)
+            *reinterpret_cast<uint32_t*>(dl + k0) = packed;
+        else
+            for (int u = 0; k0 + u < n - 1; ++u)
+                dl[k0 + u] = static_cast<uint8_t>(packed >> (8 * u));
+    }
+
+    // one bit per byte of four 0x00 / 0xff bytes, byte 0 to bit 0
+    __device__ __forceinline__ uint32_t movemask4(const uint32_t m) { return ((m & 0x80808080u) * 0x00204081u) >> 28; }
+
+    // Byte compares without SIMD instructions, exact for bytes below 128 (every dl byte is
+    // at most 95): with bit 7 set in each byte first, subtracting a byte below 128 borrows
+    // from no other byte, and leaves bit 7 clear exactly where the byte was the smaller.
+    // bits of four bytes below lim (each byte of lim <= 128)
+    __device__ __forceinline__ uint32_t lt_mask4(const uint32_t x, const uint32_t lim)
+    {
+        return movemask4(~((x | 0x80808080u) - lim));
+    }
+
+    // 16 bytes: bit t set where byte t is below each byte of lim / equal to each byte of q
+    __device__ __forceinline__ uint32_t lt_mask16(const uint4 w, const uint32_t lim)
+    {
+        return lt_mask4(w.x, lim) | (lt_mask4(w.y, lim) << 4) | (lt_mask4(w.z, lim) << 8) | (lt_mask4(w.w, lim) << 12);
+    }
+
+    __device__ __forceinline__ uint32_t eq_mask16(const uint4 w, const uint32_t q)
+    {
+        return lt_mask4(w.x ^ q, 0x01010101u) | (lt_mask4(w.y ^ q, 0x01010101u) << 4)
+               | (lt_mask4(w.z ^ q, 0x01010101u) << 8) | (lt_mask4(w.w ^ q, 0x01010101u) << 12);
+    }
+
+    // The record of binary node i (Karras 2012) with range [lo, hi], split after gamma and
+    // common prefix dnode bits, and whether it is an octree node. The range is bounded by
+    // two splits, dmin at i's end and dfar at the other (-1 past either end of the array),
+    // both below its own; its parent splits at the larger of the two (the smallest range
+    // that strictly contains [lo, hi] ends where the shared prefix first shortens), so the
+    // parent's prefix is known without a parent array. A node is an octree node when its
+    // level exceeds its parent's, or it is the root.
+    __device__ __forceinline__ void write_radix_node(const int i, const int lo, const int hi, const int gamma,
+                                                     const int dnode, const int dmin, const int dfar,
+                                                     int2* __restrict__ child, int2* __restrict__ range,
+                                                     int* __restrict__ prefix, uint32_t* __restrict__ flag)
+    {
+        child[i] = make_int2(lo == gamma ? ~gamma : gamma, hi == gamma + 1 ? ~(gamma + 1) : gamma + 1);
         range[i] = make_int2(lo, hi);
         const int pre = dnode - 1;      // codes are 63-bit: the top key bit is always shared
         prefix[i] = pre;
-        // the bound at i's end of the range is delta(i, i - d), already known as dmin; the
-        // bound at j's end is delta(j, j + d) (-1 past either end of the array)
-        const int up = max(dmin, kw.delta(kw.at(j), j, j + d)) - 1;
+        const int up = max(dmin, dfar) - 1;
         flag[i] = (i == 0 || level_of(pre) > level_of(up)) ? 1u : 0u;
+    }
+
+    // Radix-tree nodes whose ranges end within about kNearScan keys (97.5 % of them at 16.8M
+    // disk + halo bodies), found without searches. Node i extends in direction d while the
+    // adjacent prefixes stay above dmin = delta(i, i - d), so its far end is the first byte
+    // of dl beyond i (in that direction) that is <= dmin: 16 bytes are compared at a time.
+    // Its split is the one position of its range's least prefix, dnode = delta(i, j): the
+    // first byte equal to dnode from the range's low end. A node whose end lies farther goes
+    // to far_list for radix_far_kernel, so that no warp waits on one lane's long search
+    // (Karras's searches for every node took 0.47 ms at 16.8M bodies, these two kernels and
+    // the prefix bytes 0.40).
+    constexpr int kNearScan = 64;
+    constexpr int kNearChunks = kNearScan / 16 + 1;
+
+    // Node i by the byte scans: false when its record is written, true when its range ends
+    // too far for them
+    __device__ __forceinline__ bool near_node(const uint64_t* __restrict__ keys, const uint8_t* __restrict__ dl,
+                                              const int n, const int i, int2* __restrict__ child,
+                                              int2* __restrict__ range, int* __restrict__ prefix,
+                                              uint32_t* __restrict__ flag, unsigned* __restrict__ err)
+    {
+        const int dr = dl[i];
+        const int dlf = i > 0 ? static_cast<int>(dl[i - 1]) : -1;
+        const int d = dr - dlf >= 0 ? 1 : -1;
+        const int dmin = d > 0 ? dlf : dr;
+        int j = -1;
+        if (dmin >= 0)
+        {
+            const uint32_t rep = static_cast<uint32_t>(dmin + 1) * 0x01010101u;     // bytes <= dmin
+            if (d > 0)
+            {
+                // the first p >= i with dl[p] <= dmin, or n - 1 (past the last pair)
+                for (int c = 0; c < kNearChunks; ++c)
+                {
+                    const int base = (i & ~15) + 16 * c;
+                    uint32_t mk = base < n - 1 ? lt_mask16(*reinterpret_cast<const uint4*>(dl + base), rep) : 0u;
+                    if (c == 0)
+                        mk &= ~((1u << (i & 15)) - 1u);
+                    const int past = n - 1 - base;      // bytes from here on are past the last pair
+                    if (past < 16)
+                        mk |= past <= 0 ? 0xffffu : (0xffffu << past) & 0xffffu;
+                    if (mk)
+                    {
+                        j = base + __ffs(mk) - 1;
+                        break;
+                    }
+                }
+            }
+            else
+            {
+                // the last p <= i - 1 with dl[p] <= dmin, plus one; or 0 (before the first)
+                for (int c = 0; c < kNearChunks; ++c)
+                {
+                    const int base = ((i - 1) & ~15) - 16 * c;
+                    if (base < 0)
+                    {
+                        j = 0;
+                        break;
+                    }
+                    uint32_t mk = lt_mask16(*reinterpret_cast<const uint4*>(dl + base), rep);
+                    if (c == 0)
+                        mk &= (2u << ((i - 1) & 15)) - 1u;
+                    if (mk)
+                    {
+                        j = base + (31 - __clz(mk)) + 1;
+                        break;
+                    }
+                    if (base == 0)
+                    {
+                        j = 0;
+                        break;
+                    }
+                }
+            }
+        }
+        if (j < 0)
+            return true;
+        const int lo = min(i, j), hi = max(i, j);
+        const int dnode = delta(keys, n, i, j);
+        const uint32_t rq = static_cast<uint32_t>(dnode) * 0x01010101u;
+        int gamma = -1;
+        for (int c = 0; c < kNearChunks + 1; ++c)
+        {
+            const int base = (lo & ~15) + 16 * c;
+            if (base > n - 2)
+                break;      // past the last pair: the split was not found
+            uint32_t mk = eq_mask16(*reinterpret_cast<const uint4*>(dl + base), rq);
+            if (c == 0)
+                mk &= ~((1u << (lo & 15)) - 1u);
+            if (mk)
+            {
+                gamma = base + __ffs(mk) - 1;
+                break;
+            }
+        }
+        if (gamma < lo || gamma >= hi)
+        {
+            atomicOr(err, DEV_ERR_BOUNDS);      // a range without its split: not sorted keys
+            return false;
+        }
+        const int dfar = d > 0 ? (j < n - 1 ? static_cast<int>(dl[j]) : -1) : (j > 0 ? static_cast<int>(dl[j - 1]) : -1);
+        write_radix_node(i, lo, hi, gamma, dnode, dmin, dfar, child, range, prefix, flag);
+        return false;
+    }
+
+    __global__ void __launch_bounds__(256) radix_near_kernel(
+        const uint64_t* __restrict__ keys, const uint8_t* __restrict__ dl, const int n, int2* __restrict__ child,
+        int2* __restrict__ range, int* __restrict__ prefix, uint32_t* __restrict__ flag, int* __restrict__ far_list,
+        unsigned* __restrict__ far_count, unsigned* __restrict__ err)
+    {
+        const int i = blockIdx.x * 256 + threadIdx.x;
+        const bool far = i < n - 1 && near_node(keys, dl, n, i, child, range, prefix, flag, err);
+        // a warp's far nodes take consecutive slots of far_list: one global atomic a warp
+        const unsigned fm = __ballot_sync(0xffffffffu, far);
+        if (!fm)
+            return;
+        const int lane = threadIdx.x & 31, leader = __ffs(fm) - 1;
+        unsigned base = 0;
+        if (lane == leader)
+            base = atomicAdd(far_count, static_cast<unsigned>(__popc(fm)));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (far)
+            far_list[base + __popc(fm & ((1u << lane) - 1u))] = i;
+    }
+
+    // The nodes radix_near_kernel passed on, one per thread: Karras's searches (an
+    // exponential search for the range's far end, binary searches for it and the split).
+    __global__ void __launch_bounds__(256) radix_far_kernel(const uint64_t* __restrict__ keys, const int n,
+                                                            const int* __restrict__ far_list,
+                                                            const unsigned* __restrict__ far_count,
+                                                            int2* __restrict__ child, int2* __restrict__ range,
+                                                            int* __restrict__ prefix, uint32_t* __restrict__ flag)
+    {
+        const int count = static_cast<int>(*far_count);
+        for (int q = blockIdx.x * 256 + threadIdx.x; q < count; q += gridDim.x * 256)
+        {
+            const int i = far_list[q];
+            const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+            const int dmin = delta(keys, n, i, i - d);
+            int lmax = 2;
+            while (delta(keys, n, i, i + lmax * d) > dmin)
+                lmax <<= 1;
+            int l = 0;
+            for (int t = lmax >> 1; t >= 1; t >>= 1)
+                if (delta(keys, n, i, i + (l + t) * d) > dmin)
+                    l += t;
+            const int j = i + l * d;
+            const int dnode = delta(keys, n, i, j);
+            int s = 0;
+            for (int t = (l + 1) >> 1;; t = (t + 1) >> 1)
+            {
+                if (delta(keys, n, i, i + (s + t) * d) > dnode)
+                    s += t;
+                if (t == 1)
+                    break;
+            }
+            const int gamma = i + s * d + min(d, 0);
+            write_radix_node(i, min(i, j), max(i, j), gamma, dnode, dmin, delta(keys, n, j, j + d), child, range,
+                             prefix, flag);
+        }
     }
 
     // ------------------------------------------------------------------------------------
@@ -1832,9 +1987,23 @@ namespace nbg
             return NBODY_OK;
         }
         const int m = ni - 1;
-        karras_kernel<<<ceil_div(m, kKarrasThreads), kKarrasThreads, 0, s>>>(keys, ni, b.child, b.range, b.prefix,
-                                                                            b.octflag);
-        ++L;
+        {
+            // adjacent prefix lengths and the far nodes' list live in the sort's other key and
+            // value buffers, free until the next build
+            const int other = in_alt ? 0 : 1;
+            uint8_t* dl = reinterpret_cast<uint8_t*>(b.keys[other]);
+            int* far_list = reinterpret_cast<int*>(b.vals[other]);
+            unsigned* far_count = reinterpret_cast<unsigned*>(b.stats + 5);
+            adjacent_prefix_kernel<<<ceil_div(m, 256 * 4), 256, 0, s>>>(keys, ni, dl);
+            ++L;
+            radix_near_kernel<<<ceil_div(m, 256), 256, 0, s>>>(keys, dl, ni, b.child, b.range, b.prefix, b.octflag,
+                                                               far_list, far_count, ctx->dev_error);
+            ++L;
+            radix_far_kernel<<<std::min(ceil_div(m, 256), 2048u), 256, 0, s>>>(keys, ni, far_list, far_count,
+                                                                                  b.child, b.range, b.prefix,
+                                                                                  b.octflag);
+            ++L;
+        }
         e = exclusive_scan<uint32_t>(b.octflag, b.octidx, m, static_cast<uint32_t*>(scan_temp), s, &L);
         if (e != cudaSuccess)
             return ctx_cuda_fail(ctx, e, "octree compaction");
