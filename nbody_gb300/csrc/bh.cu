@@ -861,7 +861,10 @@ namespace nbg
             const int i = far_list[q];
             const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
             const int dmin = delta(keys, n, i, i - d);
-            int lmax = 2;
+            // the byte scan found the range longer than kNearScan: the doubling starts there
+            // (any start works, the binary search below only needs the range to end before
+            // i + lmax * d)
+            int lmax = kNearScan;
             while (delta(keys, n, i, i + lmax * d) > dmin)
                 lmax <<= 1;
             int l = 0;
