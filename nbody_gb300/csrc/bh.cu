@@ -61,7 +61,7 @@ namespace nbg
         // group walk: warps per CTA, list entries and stacked parent cells per warp (the
         // stack grows by at most 28 parents per tree level, 22 levels: 616 < 768)
         constexpr int kListWarps = 4;
-        constexpr int kListCap = 256;       // interaction-list entries per warp
+        constexpr int kListCap = 512;       // interaction-list entries per warp (8 KB; five CTAs per SM)
         constexpr int kGroupStack = 768;
         constexpr int kRuns = 4;            // runs (own acceptance boxes) per group
         constexpr int kBboxBlocks = 1024;
