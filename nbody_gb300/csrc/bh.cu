@@ -61,7 +61,11 @@ namespace nbg
         // group walk: warps per CTA, list entries and stacked parent cells per warp (the
         // stack grows by at most 28 parents per tree level, 22 levels: 616 < 768)
         constexpr int kListWarps = 4;
-        constexpr int kListCap = 512;       // interaction-list entries per warp (8 KB; five CTAs per SM)
+        // interaction-list entries per warp: the long list (8 KB; five CTAs per SM) drains half
+        // as often, the short one (4 KB; six CTAs) keeps more warps resident when the groups
+        // are too few to fill them
+        constexpr int kListLong = 512;
+        constexpr int kListShort = 256;
         constexpr int kGroupStack = 768;
         constexpr int kRuns = 4;            // runs (own acceptance boxes) per group
         constexpr int kBboxBlocks = 1024;
@@ -1514,7 +1518,7 @@ namespace nbg
     // tree codes (Barnes 1990's grouping; Bonsai, Bedorf et al. 2012): the walk decides each
     // cell once for the whole group and appends the sources it yields -- accepted cells as
     // (com, mass), leaves and the bodies of opened buckets as (x, m) -- to an interaction list
-    // in shared memory, which every kListCap entries is applied to every target of the group
+    // in shared memory, which every CAP entries is applied to every target of the group
     // with the direct sum's packed loop: no selection and no per-target test.
     //
     // The acceptance box. The group is split at the NSG - 1 largest jumps of its Morton codes
@@ -1534,7 +1538,7 @@ namespace nbg
     // Each target's sources refine the cells the reference's walk accepts for it alone (a
     // cell opened for the group may be one the target would have accepted), so each target
     // is summed at least as finely as in the reference, over more interactions.
-    template <int LAW, int Q, int NSG>
+    template <int LAW, int Q, int NSG, int CAP>
     __global__ void __launch_bounds__(kListWarps * 32) traverse_list_kernel(
         const OctNode* __restrict__ nodes, const float4* __restrict__ spm, const float* __restrict__ srad,
         const uint64_t* __restrict__ codes, const uint32_t* __restrict__ order, const int n, const float G,
@@ -1544,7 +1548,7 @@ namespace nbg
         constexpr int H = 2 * Q;                    // target slots per lane
         constexpr int TW = 32 * H;                  // targets per group
         static_assert(NSG >= 1 && NSG <= 32, "runs per group");
-        __shared__ __align__(16) float4 list_mem[kListWarps][kListCap];
+        __shared__ __align__(16) float4 list_mem[kListWarps][CAP];
         __shared__ int stack_mem[kListWarps][kGroupStack];
         __shared__ __align__(16) float4 box_mem[kListWarps][2 * NSG];
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1684,7 +1688,7 @@ namespace nbg
             // append one source per flagged lane, draining first when the list would overflow
             auto append = [&](const bool take, const float4 src) {
                 const unsigned m = __ballot_sync(0xffffffffu, take);
-                if (ln + __popc(m) > kListCap)
+                if (ln + __popc(m) > CAP)
                     drain();
                 if (take)
                     list[ln + __popc(m & lt)] = src;
@@ -2066,12 +2070,20 @@ namespace nbg
             const bool soft = p->law == NBODY_LAW_SOFTENED;
             using Walk = void (*)(const OctNode*, const float4*, const float*, const uint64_t*, const uint32_t*, int,
                                   float, float, float4*, float*, unsigned*, unsigned long long*);
-            Walk f64 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 1, kRuns>
-                            : traverse_list_kernel<NBODY_LAW_CUTOFF, 1, kRuns>;
-            Walk f128 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 2, kRuns>
-                             : traverse_list_kernel<NBODY_LAW_CUTOFF, 2, kRuns>;
-            Walk f256 = soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 4, kRuns>
-                             : traverse_list_kernel<NBODY_LAW_CUTOFF, 4, kRuns>;
+            // [group 64, 128, 256][short, long list]
+            const Walk fns[3][2] = {
+                { soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 1, kRuns, kListShort>
+                       : traverse_list_kernel<NBODY_LAW_CUTOFF, 1, kRuns, kListShort>,
+                  soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 1, kRuns, kListLong>
+                       : traverse_list_kernel<NBODY_LAW_CUTOFF, 1, kRuns, kListLong> },
+                { soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 2, kRuns, kListShort>
+                       : traverse_list_kernel<NBODY_LAW_CUTOFF, 2, kRuns, kListShort>,
+                  soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 2, kRuns, kListLong>
+                       : traverse_list_kernel<NBODY_LAW_CUTOFF, 2, kRuns, kListLong> },
+                { soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 4, kRuns, kListShort>
+                       : traverse_list_kernel<NBODY_LAW_CUTOFF, 4, kRuns, kListShort>,
+                  soft ? traverse_list_kernel<NBODY_LAW_SOFTENED, 4, kRuns, kListLong>
+                       : traverse_list_kernel<NBODY_LAW_CUTOFF, 4, kRuns, kListLong> } };
             auto per_sm = [&](Walk fn) {
                 int per = 0;
                 if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kListWarps * 32, 0) != cudaSuccess || per < 1)
@@ -2081,10 +2093,13 @@ namespace nbg
             const char* gsel = std::getenv("NBODY_CUDA_BH_GROUP");
             int group = gsel ? std::atoi(gsel) : 0;
             if (group != 64 && group != 128 && group != 256)
-                group = static_cast<long long>(ni) >= 128LL * per_sm(f128) * sms * kListWarps ? 128 : 64;
-            const Walk fn = group == 256 ? f256 : (group == 128 ? f128 : f64);
-            const int per = per_sm(fn);
+                group = static_cast<long long>(ni) >= 128LL * per_sm(fns[1][0]) * sms * kListWarps ? 128 : 64;
+            const int gi = group == 256 ? 2 : (group == 128 ? 1 : 0);
             const int groups = (ni + group - 1) / group;
+            // the long list once the groups are at least twice the warps it leaves resident
+            const bool long_list = groups >= 2LL * per_sm(fns[gi][1]) * sms * kListWarps;
+            const Walk fn = fns[gi][long_list ? 1 : 0];
+            const int per = per_sm(fn);
             const int grid = std::min((groups + kListWarps - 1) / kListWarps, sms * per);
             fn<<<grid, kListWarps * 32, 0, s>>>(b.nodes, b.spm, b.srad, b.codes, b.order, ni, p->G, p->eps2, acc,
                                                 body_out, ctx->dev_error, b.stats);
