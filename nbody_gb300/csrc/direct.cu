@@ -321,14 +321,18 @@ namespace nbg
     }
 
     // Sum jsplit chunk partials in chunk order into acc (SoA float4) or Body::acc (AoS).
+    template <int W>
     __global__ void reduce_partials_kernel(const float4* __restrict__ part, const int jsplit,
                                            const int n, const float G, float4* __restrict__ acc,
                                            float* __restrict__ body_out)
     {
-        const int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i >= n)
+        const int t = blockIdx.x * blockDim.x + threadIdx.x;
+        const int i = t / W, g = t % W;
+        if (W == 1 && i >= n)
             return;
-        const float3 a = combine_partials(part, part + n, jsplit, n, i, G);
+        const float3 a = combine_partials_w<W>(part, part + n, jsplit, n, min(i, n - 1), g, G);
+        if (i >= n || g != 0)
+            return;
         if (body_out)
         {
             float* b = body_out + static_cast<size_t>(i) * 12 + 8;
@@ -555,7 +559,11 @@ namespace nbg
     cudaError_t launch_reduce(const float4* scratch, const int jsplit, const int n, const float G, float4* acc,
                               float* body_out, cudaStream_t stream, uint64_t* launches)
     {
-        reduce_partials_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(scratch, jsplit, n, G, acc, body_out);
+        if (combine_width(n, jsplit) == 8)
+            reduce_partials_kernel<8><<<ceil_div(static_cast<size_t>(n) * 8, 256), 256, 0, stream>>>(
+                scratch, jsplit, n, G, acc, body_out);
+        else
+            reduce_partials_kernel<1><<<ceil_div(n, 256), 256, 0, stream>>>(scratch, jsplit, n, G, acc, body_out);
         ++*launches;
         return cudaGetLastError();
     }

@@ -38,12 +38,18 @@ namespace nbg
     // scaled by G: the same formula for one chunk or many, so the result does not depend on
     // how the sources were split. FP32 only: GB300's FP64 pipe runs at 1/64 of the FP32
     // rate, and a small system's few bodies would put that work on a few SMs.
-    __device__ __forceinline__ float3 combine_partials(const float4* __restrict__ S, const float4* __restrict__ C,
-                                                       const int js, const int n, const int i, const float G)
+    // W lanes per body (consecutive lanes of one warp, g = lane % W): lane g sums chunks g,
+    // g + W, ... as above, and the lanes' double-float sums are then merged pairwise in a
+    // fixed order (the same TwoSum step). Every lane of the warp must call it; the result is
+    // lane g = 0's. W = 1 is the plain sequential sum.
+    template <int W>
+    __device__ __forceinline__ float3 combine_partials_w(const float4* __restrict__ S, const float4* __restrict__ C,
+                                                         const int js, const int n, const int i, const int g,
+                                                         const float G)
     {
         float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
 #pragma unroll 4
-        for (int c = 0; c < js; ++c)
+        for (int c = g; c < js; c += W)
         {
             const size_t k = 2 * static_cast<size_t>(c) * n + i;
             const float4 s = S[k], e = C[k];
@@ -58,8 +64,36 @@ namespace nbg
             sz = t;
             ez = __fadd_rn(ez, __fadd_rn(r, e.z));
         }
+#pragma unroll
+        for (int off = W / 2; off > 0; off >>= 1)
+        {
+            const float osx = __shfl_down_sync(0xffffffffu, sx, off, W), oex = __shfl_down_sync(0xffffffffu, ex, off, W);
+            const float osy = __shfl_down_sync(0xffffffffu, sy, off, W), oey = __shfl_down_sync(0xffffffffu, ey, off, W);
+            const float osz = __shfl_down_sync(0xffffffffu, sz, off, W), oez = __shfl_down_sync(0xffffffffu, ez, off, W);
+            float t, r;
+            two_sum(sx, osx, t, r);
+            sx = t;
+            ex = __fadd_rn(ex, __fadd_rn(r, oex));
+            two_sum(sy, osy, t, r);
+            sy = t;
+            ey = __fadd_rn(ey, __fadd_rn(r, oey));
+            two_sum(sz, osz, t, r);
+            sz = t;
+            ez = __fadd_rn(ez, __fadd_rn(r, oez));
+        }
         return make_float3(G * __fadd_rn(sx, ex), G * __fadd_rn(sy, ey), G * __fadd_rn(sz, ez));
     }
+
+    __device__ __forceinline__ float3 combine_partials(const float4* __restrict__ S, const float4* __restrict__ C,
+                                                       const int js, const int n, const int i, const float G)
+    {
+        return combine_partials_w<1>(S, C, js, n, i, 0, G);
+    }
+
+    // Lanes per body for the combine: a small system has many chunks and few bodies, so eight
+    // lanes a body spread the combine over eight times the SMs. A function of (n, js) only,
+    // so the sums do not depend on which kernel combines them.
+    inline int combine_width(const int n, const int js) { return (js >= 8 && n <= (1 << 16)) ? 8 : 1; }
 
     // Pick a launch shape for n bodies. force_variant >= 0 pins the (T, block) entry.
     DirectPlan plan_direct(size_t n, int law, bool aos, int force_variant = -1);

@@ -27,26 +27,30 @@ namespace nbg
         x = __fadd_rn(x, __fmul_rn(v, dt));
     }
 
+    // W lanes per body combine the partials (combine_partials_w); lane 0 integrates
+    template <int W>
     __global__ void integrate_soa_kernel(float4* __restrict__ pm, float4* __restrict__ vr,
                                          float4* __restrict__ acc, const float4* __restrict__ part,
                                          const int js, const int n, const float G, const float dt,
                                          const float size, const int wrap)
     {
-        const int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i >= n)
+        const int t = blockIdx.x * blockDim.x + threadIdx.x;
+        const int i = t / W, g = t % W;
+        if (W == 1 && i >= n)
+            return;
+        float3 a = make_float3(0.f, 0.f, 0.f);
+        if (part)
+            a = combine_partials_w<W>(part, part + n, js, n, min(i, n - 1), g, G);
+        if (i >= n || g != 0)
             return;
         float4 p = pm[i];
         float4 v = vr[i];
-        float3 a;
         if (part)
-        {
-            a = combine_partials(part, part + n, js, n, i, G);
             acc[i] = make_float4(a.x, a.y, a.z, 0.f);
-        }
         else
         {
-            const float4 t = acc[i];
-            a = make_float3(t.x, t.y, t.z);
+            const float4 t4 = acc[i];
+            a = make_float3(t4.x, t4.y, t4.z);
         }
         euler(p.x, v.x, a.x, dt);
         euler(p.y, v.y, a.y, dt);
@@ -61,12 +65,19 @@ namespace nbg
         vr[i] = v;
     }
 
+    template <int W>
     __global__ void integrate_aos_kernel(float* __restrict__ bodies, const float4* __restrict__ part,
                                          const int js, const int n, const float G, const float dt,
                                          const float size, const int wrap)
     {
-        const int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i >= n)
+        const int t = blockIdx.x * blockDim.x + threadIdx.x;
+        const int i = t / W, g = t % W;
+        if (W == 1 && i >= n)
+            return;
+        float3 s = make_float3(0.f, 0.f, 0.f);
+        if (part)
+            s = combine_partials_w<W>(part, part + n, js, n, min(i, n - 1), g, G);
+        if (i >= n || g != 0)
             return;
         float4* b = reinterpret_cast<float4*>(bodies) + static_cast<size_t>(i) * 3;
         float4 p = b[0];    // pos, radius
@@ -74,7 +85,6 @@ namespace nbg
         float4 a = b[2];    // acc, pad
         if (part)
         {
-            const float3 s = combine_partials(part, part + n, js, n, i, G);
             a.x = s.x;
             a.y = s.y;
             a.z = s.z;
@@ -135,8 +145,12 @@ namespace nbg
     {
         if (n <= 0)
             return cudaSuccess;
-        integrate_soa_kernel<<<ceil_div(n, kBlock), kBlock, 0, stream>>>(pm, vr, acc, part, js, n, G, dt, size,
-                                                                          wrap);
+        if (part && combine_width(n, js) == 8)
+            integrate_soa_kernel<8><<<ceil_div(static_cast<size_t>(n) * 8, kBlock), kBlock, 0, stream>>>(
+                pm, vr, acc, part, js, n, G, dt, size, wrap);
+        else
+            integrate_soa_kernel<1><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(pm, vr, acc, part, js, n, G, dt, size,
+                                                                             wrap);
         ++*launches;
         return cudaGetLastError();
     }
@@ -147,7 +161,12 @@ namespace nbg
     {
         if (n <= 0)
             return cudaSuccess;
-        integrate_aos_kernel<<<ceil_div(n, kBlock), kBlock, 0, stream>>>(bodies, part, js, n, G, dt, size, wrap);
+        if (part && combine_width(n, js) == 8)
+            integrate_aos_kernel<8><<<ceil_div(static_cast<size_t>(n) * 8, kBlock), kBlock, 0, stream>>>(
+                bodies, part, js, n, G, dt, size, wrap);
+        else
+            integrate_aos_kernel<1><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(bodies, part, js, n, G, dt, size,
+                                                                             wrap);
         ++*launches;
         return cudaGetLastError();
     }
