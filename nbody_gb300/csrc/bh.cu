@@ -655,10 +655,11 @@ namespace nbg
 
     __device__ __forceinline__ int level_of(const int prefix) { return min(kMaxLevel, prefix / 3); }
 
-    // dl[k] = delta(k, k + 1) for k < n - 1: 1 .. 95, one byte. Four per thread. For sorted
-    // keys the common prefix of keys i < j is the least of dl[i .. j - 1].
+    // dl[k] = delta(k, k + 1) for k < n - 1: 1 .. 95, one byte, and smp[k] = the key at 64 k
+    // for 64 k < n - 1. Four per thread. For sorted keys the common prefix of keys i < j is
+    // the least of dl[i .. j - 1].
     __global__ void __launch_bounds__(256) adjacent_prefix_kernel(const uint64_t* __restrict__ keys, const int n,
-                                                                  uint8_t* __restrict__ dl)
+                                                                  uint8_t* __restrict__ dl, uint64_t* __restrict__ smp)
     {
         const int k0 = (blockIdx.x * 256 + threadIdx.x) * 4;
         if (k0 >= n - 1)
@@ -667,6 +668,8 @@ namespace nbg
 #pragma unroll
         for (int u = 0; u < 5; ++u)
             a[u] = keys[min(k0 + u, n - 1)];
+        if ((k0 & 63) == 0)
+            smp[k0 >> 6] = a[0];        // every 64th key, for the far nodes' coarse searches
         uint32_t packed = 0;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
@@ -851,43 +854,139 @@ namespace nbg
             far_list[base + __popc(fm & ((1u << lane) - 1u))] = i;
     }
 
-    // The nodes radix_near_kernel passed on, one per thread: Karras's searches (an
-    // exponential search for the range's far end, binary searches for it and the split).
-    __global__ void __launch_bounds__(256) radix_far_kernel(const uint64_t* __restrict__ keys, const int n,
+    __device__ __forceinline__ int delta_of(const uint64_t a, const int i, const uint64_t b, const int j)
+    {
+        return a != b ? __clzll(static_cast<long long>(a ^ b))
+                      : 64 + __clz(static_cast<int>(static_cast<unsigned>(i) ^ static_cast<unsigned>(j)));
+    }
+
+    // The first p >= start with dl[p] <= D (n - 1 when none: past the last pair), given
+    // dl[ref .. start - 1] > D and kref = key ref. A coarse search over every 64th key finds
+    // the last sampled position P with delta(ref, P) > D, that is dl[ref .. P - 1] > D
+    // (exponential, then binary); the answer lies in the 64 bytes after it, found by the
+    // byte scan. The samples are 1/64 of the keys and stay in the caches.
+    __device__ int first_le_up(const uint64_t* __restrict__ smp, const uint8_t* __restrict__ dl, const int n,
+                               const uint64_t kref, const int ref, const int start, const int D,
+                               unsigned* __restrict__ err)
+    {
+        auto f = [&](const int k) {
+            const int P = 64 * k;
+            return P < n - 1 && delta_of(kref, ref, smp[k], P) > D;
+        };
+        int q0 = start;
+        const int ka = (start >> 6) + 1;
+        if (f(ka))
+        {
+            int lo = ka, step = 1;
+            while (f(lo + step))
+            {
+                lo += step;
+                step <<= 1;
+            }
+            int hi = lo + step;
+            while (hi - lo > 1)
+            {
+                const int mid = (lo + hi) >> 1;
+                if (f(mid))
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            q0 = 64 * lo;
+        }
+        const uint32_t lim = static_cast<uint32_t>(D + 1) * 0x01010101u;      // bytes <= D
+        for (int c = 0; c < 8; ++c)
+        {
+            const int base = (q0 & ~15) + 16 * c;
+            uint32_t mk = base < n - 1 ? lt_mask16(*reinterpret_cast<const uint4*>(dl + base), lim) : 0u;
+            if (c == 0)
+                mk &= ~((1u << (q0 & 15)) - 1u);
+            const int past = n - 1 - base;
+            if (past < 16)
+                mk |= past <= 0 ? 0xffffu : (0xffffu << past) & 0xffffu;
+            if (mk)
+                return base + __ffs(mk) - 1;
+        }
+        atomicOr(err, DEV_ERR_BOUNDS);      // not sorted keys
+        return n - 1;
+    }
+
+    // The last p <= start with dl[p] <= D (-1 when none), given dl[start + 1 .. ref - 1] > D;
+    // the same coarse search downward (delta(ref, P) > D means dl[P .. ref - 1] > D).
+    __device__ int last_le_down(const uint64_t* __restrict__ smp, const uint8_t* __restrict__ dl, const uint64_t kref,
+                                const int ref, const int start, const int D, unsigned* __restrict__ err)
+    {
+        auto f = [&](const int k) { return k >= 0 && delta_of(kref, ref, smp[k], 64 * k) > D; };
+        int q0 = start;
+        const int ka = start >> 6;
+        if (f(ka))
+        {
+            int hi = ka, step = 1;
+            while (f(hi - step))
+            {
+                hi -= step;
+                step <<= 1;
+            }
+            int lo = hi - step;
+            while (hi - lo > 1)
+            {
+                const int mid = (lo + hi) >> 1;
+                if (f(mid))
+                    hi = mid;
+                else
+                    lo = mid;
+            }
+            q0 = 64 * hi - 1;
+        }
+        const uint32_t lim = static_cast<uint32_t>(D + 1) * 0x01010101u;
+        for (int c = 0; c < 8; ++c)
+        {
+            const int base = (q0 & ~15) - 16 * c;
+            if (q0 < 0 || base < 0)
+                return -1;
+            uint32_t mk = lt_mask16(*reinterpret_cast<const uint4*>(dl + base), lim);
+            if (c == 0)
+                mk &= (2u << (q0 & 15)) - 1u;
+            if (mk)
+                return base + 31 - __clz(mk);
+        }
+        atomicOr(err, DEV_ERR_BOUNDS);
+        return -1;
+    }
+
+    // The nodes radix_near_kernel passed on, one per thread: the range's far end and the
+    // split by the coarse-then-fine searches above (the top levels' nodes span millions of
+    // keys; their searches over the samples stay in the caches).
+    __global__ void __launch_bounds__(256) radix_far_kernel(const uint64_t* __restrict__ keys,
+                                                            const uint8_t* __restrict__ dl,
+                                                            const uint64_t* __restrict__ smp, const int n,
                                                             const int* __restrict__ far_list,
                                                             const unsigned* __restrict__ far_count,
                                                             int2* __restrict__ child, int2* __restrict__ range,
-                                                            int* __restrict__ prefix, uint32_t* __restrict__ flag)
+                                                            int* __restrict__ prefix, uint32_t* __restrict__ flag,
+                                                            unsigned* __restrict__ err)
     {
         const int count = static_cast<int>(*far_count);
         for (int q = blockIdx.x * 256 + threadIdx.x; q < count; q += gridDim.x * 256)
         {
             const int i = far_list[q];
-            const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
-            const int dmin = delta(keys, n, i, i - d);
-            // the byte scan found the range longer than kNearScan: the doubling starts there
-            // (any start works, the binary search below only needs the range to end before
-            // i + lmax * d)
-            int lmax = kNearScan;
-            while (delta(keys, n, i, i + lmax * d) > dmin)
-                lmax <<= 1;
-            int l = 0;
-            for (int t = lmax >> 1; t >= 1; t >>= 1)
-                if (delta(keys, n, i, i + (l + t) * d) > dmin)
-                    l += t;
-            const int j = i + l * d;
+            const uint64_t ki = keys[i];
+            const int dr = dl[i];
+            const int dlf = i > 0 ? static_cast<int>(dl[i - 1]) : -1;
+            const int d = dr - dlf >= 0 ? 1 : -1;
+            const int dmin = d > 0 ? dlf : dr;
+            const int j = d > 0 ? first_le_up(smp, dl, n, ki, i, i, dmin, err)
+                                : last_le_down(smp, dl, ki, i, i - 1, dmin, err) + 1;
+            const int lo = min(i, j), hi = max(i, j);
             const int dnode = delta(keys, n, i, j);
-            int s = 0;
-            for (int t = (l + 1) >> 1;; t = (t + 1) >> 1)
+            const int gamma = first_le_up(smp, dl, n, keys[lo], lo, lo, dnode, err);
+            if (gamma < lo || gamma >= hi)
             {
-                if (delta(keys, n, i, i + (s + t) * d) > dnode)
-                    s += t;
-                if (t == 1)
-                    break;
+                atomicOr(err, DEV_ERR_BOUNDS);
+                continue;
             }
-            const int gamma = i + s * d + min(d, 0);
-            write_radix_node(i, min(i, j), max(i, j), gamma, dnode, dmin, delta(keys, n, j, j + d), child, range,
-                             prefix, flag);
+            const int dfar = d > 0 ? (j < n - 1 ? static_cast<int>(dl[j]) : -1) : (j > 0 ? static_cast<int>(dl[j - 1]) : -1);
+            write_radix_node(i, lo, hi, gamma, dnode, dmin, dfar, child, range, prefix, flag);
         }
     }
 
@@ -1995,20 +2094,22 @@ namespace nbg
         }
         const int m = ni - 1;
         {
-            // adjacent prefix lengths and the far nodes' list live in the sort's other key and
-            // value buffers, free until the next build
+            // adjacent prefix lengths, key samples and the far nodes' list live in the sort's
+            // other key and value buffers, free until the next build
             const int other = in_alt ? 0 : 1;
             uint8_t* dl = reinterpret_cast<uint8_t*>(b.keys[other]);
+            // (n rounded up to 8 bytes, then n / 64 + 1 keys: within the buffer's 8 n bytes for n >= 2)
+            uint64_t* smp = reinterpret_cast<uint64_t*>(dl + ((n + 7) & ~size_t(7)));
             int* far_list = reinterpret_cast<int*>(b.vals[other]);
             unsigned* far_count = reinterpret_cast<unsigned*>(b.stats + 5);
-            adjacent_prefix_kernel<<<ceil_div(m, 256 * 4), 256, 0, s>>>(keys, ni, dl);
+            adjacent_prefix_kernel<<<ceil_div(m, 256 * 4), 256, 0, s>>>(keys, ni, dl, smp);
             ++L;
             radix_near_kernel<<<ceil_div(m, 256), 256, 0, s>>>(keys, dl, ni, b.child, b.range, b.prefix, b.octflag,
                                                                far_list, far_count, ctx->dev_error);
             ++L;
-            radix_far_kernel<<<std::min(ceil_div(m, 256), 2048u), 256, 0, s>>>(keys, ni, far_list, far_count,
+            radix_far_kernel<<<std::min(ceil_div(m, 256), 2048u), 256, 0, s>>>(keys, dl, smp, ni, far_list, far_count,
                                                                                   b.child, b.range, b.prefix,
-                                                                                  b.octflag);
+                                                                                  b.octflag, ctx->dev_error);
             ++L;
         }
         e = exclusive_scan<uint32_t>(b.octflag, b.octidx, m, static_cast<uint32_t*>(scan_temp), s, &L);
