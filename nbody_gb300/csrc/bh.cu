@@ -690,10 +690,10 @@ namespace nbg
     // one bit per byte of four 0x00 / 0xff bytes, byte 0 to bit 0
     __device__ __forceinline__ uint32_t movemask4(const uint32_t m) { return ((m & 0x80808080u) * 0x00204081u) >> 28; }
 
-    // Byte compares without SIMD instructions, exact for bytes below 128 (every dl byte is
-    // at most 95): with bit 7 set in each byte first, subtracting a byte below 128 borrows
-    // from no other byte, and leaves bit 7 clear exactly where the byte was the smaller.
-    // bits of four bytes below lim (each byte of lim <= 128)
+    // One bit for each of four bytes of x below the matching byte of lim (each <= 128),
+    // without SIMD instructions, exact for bytes below 128 (every dl byte is at most 95):
+    // with bit 7 set in each byte of x first, subtracting a byte of at most 128 borrows from
+    // no other byte, and leaves bit 7 clear exactly where x's byte was the smaller.
     __device__ __forceinline__ uint32_t lt_mask4(const uint32_t x, const uint32_t lim)
     {
         return movemask4(~((x | 0x80808080u) - lim));
@@ -738,8 +738,8 @@ namespace nbg
     // Its split is the one position of its range's least prefix, dnode = delta(i, j): the
     // first byte equal to dnode from the range's low end. A node whose end lies farther goes
     // to far_list for radix_far_kernel, so that no warp waits on one lane's long search
-    // (Karras's searches for every node took 0.47 ms at 16.8M bodies, these two kernels and
-    // the prefix bytes 0.40).
+    // (Karras's searches for every node took 0.47 ms at 16.8M bodies; these kernels and the
+    // prefix bytes take about 0.37).
     constexpr int kNearScan = 64;
     constexpr int kNearChunks = kNearScan / 16 + 1;
 
